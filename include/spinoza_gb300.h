@@ -1,0 +1,267 @@
+/*
+ * spinoza_gb300 — C ABI of the GB300-native FP64 state-vector engine.
+ *
+ * This is the drop-in boundary for Spinoza's gate-application path
+ * (QuState/spinoza v0.5.1).  Every entry point replaces one function of the
+ * reference's public Rust API; the citation above each declaration gives the
+ * reference file:line (paths relative to the reference repository).
+ *
+ * Conventions
+ *   - The state lives in HBM as two FP64 arrays (SoA): reals[2^n], imags[2^n],
+ *     exactly the layout of `State { reals, imags, n }` (spinoza/src/core.rs:20-27).
+ *   - A handle owns (or wraps) the two device arrays and one CUDA stream.  All
+ *     work on a handle is issued on that stream; calls on one handle must be
+ *     serialised by the caller (the reference borrows `&mut State`).
+ *   - Every function returns an int status (SPZ_OK == 0).  Nothing throws across
+ *     the ABI.  Where the reference panics (bad qubit index, unsupported gate,
+ *     n == 0) this library returns an error code and leaves the state untouched.
+ *   - Host pointers passed for bulk data (upload/download, uniforms, outputs) may
+ *     be pageable or pinned host memory, or device memory (UVA, cudaMemcpyDefault).
+ *   - Random draws are explicit inputs (uniforms in [0,1)), so every result is
+ *     reproducible; the reference draws from an unseeded thread_rng.
+ */
+#ifndef SPINOZA_GB300_H
+#define SPINOZA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+enum spz_status {
+  SPZ_OK = 0,
+  SPZ_ERR_INVALID_ARGUMENT = 1, /* qubit out of range, duplicate qubits, n == 0, ...   */
+  SPZ_ERR_UNSUPPORTED = 2,      /* gate/control combination without a definition      */
+  SPZ_ERR_OUT_OF_MEMORY = 3,    /* device or pinned-host allocation failed             */
+  SPZ_ERR_CUDA = 4,             /* a CUDA runtime call failed (see spz_last_error)     */
+  SPZ_ERR_NULL = 5,             /* a required pointer argument was NULL                */
+  SPZ_ERR_TIMEOUT = 6           /* a bounded device-side wait expired                  */
+};
+
+/* Human-readable text of the last error raised on the calling thread. */
+const char* spz_last_error(void);
+/* Library version string ("spinoza_gb300 <semver> sm_103a"). */
+const char* spz_version(void);
+
+/* ----------------------------------------------------------------- gates */
+/* Gate kinds; same variants and order as `enum Gate` (spinoza/src/gates.rs:45-74). */
+enum spz_gate_kind {
+  SPZ_GATE_H = 0,
+  SPZ_GATE_M = 1,       /* measurement; only valid inside spz_circuit_execute       */
+  SPZ_GATE_X = 2,
+  SPZ_GATE_Y = 3,
+  SPZ_GATE_Z = 4,
+  SPZ_GATE_P = 5,       /* p[0] = angle                                             */
+  SPZ_GATE_RX = 6,      /* p[0] = angle                                             */
+  SPZ_GATE_RY = 7,      /* p[0] = angle                                             */
+  SPZ_GATE_RZ = 8,      /* p[0] = angle                                             */
+  SPZ_GATE_SWAP = 9,    /* q0, q1 = the two swapped qubits                          */
+  SPZ_GATE_U = 10,      /* p[0..2] = theta, phi, lambda                             */
+  SPZ_GATE_UNITARY = 11,/* dense unitary: not on this path (returns UNSUPPORTED)    */
+  SPZ_GATE_BITFLIP = 12 /* p[0] = probability, p[1] = uniform draw: X iff p[1] <= p[0] */
+};
+
+/* A gate with its payload, the C form of the Rust `Gate` enum. */
+typedef struct spz_gate {
+  int32_t kind;  /* enum spz_gate_kind */
+  uint32_t q0;   /* SWAP: first qubit  */
+  uint32_t q1;   /* SWAP: second qubit */
+  uint32_t pad_;
+  double p[3];
+} spz_gate;
+
+/* ----------------------------------------------------------------- state */
+typedef struct spz_state_s* spz_state_t;
+
+/* Largest qubit count a handle accepts (2 x 2^34 x 8 B = 256 GiB of HBM). */
+#define SPZ_MAX_QUBITS 34
+
+/* State::new(n): allocate 2 x 2^n FP64 on the current device and set |0...0>.
+ * Replaces spinoza/src/core.rs:32-42 (asserts n > 0). */
+int spz_state_create(uint32_t n, spz_state_t* out);
+
+/* Wrap caller-owned device arrays (e.g. torch tensors) without copying.  The
+ * arrays must hold 2^n doubles each, 16-byte aligned; the caller keeps them
+ * alive until spz_state_destroy.  The contents are left as they are. */
+int spz_state_wrap(uint32_t n, double* d_reals, double* d_imags, spz_state_t* out);
+
+/* Release the handle (and its arrays when it owns them). */
+int spz_state_destroy(spz_state_t h);
+
+/* Issue all later work of this handle on `stream` (a cudaStream_t; NULL = the
+ * handle's own stream). */
+int spz_state_set_stream(spz_state_t h, void* stream);
+
+/* Wait until all work issued on the handle's stream has finished. */
+int spz_state_synchronize(spz_state_t h);
+
+/* n, and the device pointers of the two arrays. */
+int spz_state_num_qubits(spz_state_t h, uint32_t* n);
+int spz_state_device_arrays(spz_state_t h, double** d_reals, double** d_imags);
+
+/* Copy 2^n reals and imags in (host -> device) / out (device -> host).
+ * The Rust State exposes `pub reals, pub imags` (spinoza/src/core.rs:22-24);
+ * these two calls are how a caller reads or replaces them. */
+int spz_state_upload(spz_state_t h, const double* reals, const double* imags);
+int spz_state_download(spz_state_t h, double* reals, double* imags);
+
+/* Reset to |0...0> (the content of State::new). */
+int spz_state_reset_zero(spz_state_t h);
+
+/* dst <- src (same n).  Replaces `State: Clone` (spinoza/src/core.rs:18). */
+int spz_state_copy(spz_state_t dst, spz_state_t src);
+
+/* Fill with a seeded synthetic state.  dist 0: reals/imags i.i.d. uniform in
+ * [-1,1) from the counter-based splitmix64 stream (bit-reproducible on the
+ * host); dist 1: i.i.d. N(0,1) by Box-Muller over the same stream.  When
+ * `normalise` is non-zero the state is scaled to unit norm. */
+int spz_state_fill_random(spz_state_t h, uint64_t seed, int dist, int normalise);
+
+/* --------------------------------------------------------- gate application */
+/* apply(gate, &mut State, target): uncontrolled gate.
+ * Replaces spinoza/src/gates.rs:215-232.  SWAP takes its qubits from the gate
+ * (gates.rs:1376); BitFlipNoise applies X iff gate.p[1] <= gate.p[0]
+ * (gates.rs:1365-1374, with the draw made explicit). */
+int spz_apply(spz_state_t h, const spz_gate* gate, uint32_t target);
+
+/* c_apply(gate, &mut State, control, target).  Replaces gates.rs:257-269.
+ * Accepts every 1-qubit gate kind, including Z (controlled-Z), which the
+ * reference's match arm lacks (gates.rs:258-268). */
+int spz_c_apply(spz_state_t h, const spz_gate* gate, uint32_t control, uint32_t target);
+
+/* cc_apply(gate, &mut State, c0, c1, target).  Replaces gates.rs:272-277
+ * (the reference only defines X; this library accepts every 1-qubit gate). */
+int spz_cc_apply(spz_state_t h, const spz_gate* gate, uint32_t control0, uint32_t control1,
+                 uint32_t target);
+
+/* mc_apply(gate, &mut State, controls, zeros, target).  Replaces
+ * gates.rs:290-320.  The gate acts on `target` for basis states whose control
+ * qubits all read 1, except the qubits listed in `zeros`, which must read 0.
+ * `zeros` may be NULL (nzeros == 0); every entry of `zeros` must also appear in
+ * `controls`. */
+int spz_mc_apply(spz_state_t h, const spz_gate* gate, const uint32_t* controls,
+                 uint32_t ncontrols, const uint32_t* zeros, uint32_t nzeros, uint32_t target);
+
+/* ---------------------------------------------------------------- circuits */
+/* Control kinds of a transformation; same variants as `enum Controls`
+ * (spinoza/src/circuit.rs:55-69). */
+enum spz_controls_kind {
+  SPZ_CONTROLS_NONE = 0,
+  SPZ_CONTROLS_SINGLE = 1,
+  SPZ_CONTROLS_ONES = 2,
+  SPZ_CONTROLS_MIXED = 3
+};
+
+/* One QuantumTransformation (circuit.rs:113-120) in flat form.  For M the
+ * measurement draw is gate.p[0] (outcome 1 iff p[0] < 1 - prob0). */
+typedef struct spz_op {
+  spz_gate gate;
+  uint32_t target;
+  int32_t controls_kind; /* enum spz_controls_kind           */
+  uint64_t controls;     /* bit q set: qubit q is a control  */
+  uint64_t zeros;        /* MIXED: controls that must read 0 */
+} spz_op;
+
+/* QubitTracker (circuit.rs:122-164): which qubits were measured, and the values. */
+typedef struct spz_tracker {
+  uint64_t measured;
+  uint64_t values;
+} spz_tracker;
+
+/* Execution flags. */
+#define SPZ_EXEC_DEFAULT 0u      /* fused executor: runs of gates per shared-memory tile  */
+#define SPZ_EXEC_UNFUSED 1u      /* one kernel per gate (the plain per-gate path)         */
+#define SPZ_EXEC_TIME_PASSES 4u  /* time every pass with CUDA events (synchronises once)  */
+
+/* Execution counters filled by spz_circuit_execute (may be NULL). */
+typedef struct spz_exec_stats {
+  uint64_t gates;          /* gates applied                                         */
+  uint64_t passes;         /* passes over the state (kernel launches)               */
+  uint64_t tile_passes;    /* of which fused shared-memory tile passes              */
+  uint64_t bytes_moved;    /* HBM bytes the passes read + wrote                     */
+  uint64_t algorithmic_bytes; /* sum over gates of the unfused bytes                */
+  uint64_t fp64_ops;       /* FP64-pipe instructions the gates' arithmetic needs    */
+  double tile_ms;          /* SPZ_EXEC_TIME_PASSES: device time of the tile passes  */
+  double plain_ms;         /* SPZ_EXEC_TIME_PASSES: device time of plain gate passes */
+} spz_exec_stats;
+
+/* QuantumCircuit::execute (circuit.rs:552-600): apply `ops` in order.
+ * `tracker` carries the QubitTracker across calls (may be NULL when the list has
+ * no M and no classically controlled gate).  A Single control on an already
+ * measured qubit becomes a classical control (circuit.rs:570-578). */
+int spz_circuit_execute(spz_state_t h, const spz_op* ops, size_t nops, spz_tracker* tracker,
+                        uint32_t flags, spz_exec_stats* stats);
+
+/* Plan `ops` for an n-qubit state without running anything (host only; no
+ * device is needed): fills the counters spz_circuit_execute would, taking every
+ * measurement outcome as 0.  For inspecting how a circuit is fused. */
+int spz_plan_stats(uint32_t n, const spz_op* ops, size_t nops, uint32_t flags, spz_exec_stats* stats);
+
+/* iqft(&mut State, targets) (spinoza/src/core.rs:184-191). */
+int spz_iqft(spz_state_t h, const uint32_t* targets, uint32_t ntargets);
+
+/* ------------------------------------------------------------- measurement */
+/* measure_qubit(&mut State, target, reset, v) -> u8 (measurement.rs:12-92).
+ * forced: -1 draws the outcome from `u` (1 iff u < 1 - prob0), 0/1 forces it.
+ * *outcome receives the value; *prob0 (may be NULL) the probability of 0. */
+int spz_measure_qubit(spz_state_t h, uint32_t target, int reset, int forced, double u,
+                      uint8_t* outcome, double* prob0);
+
+/* Probability that `target` reads 0 (the first pass of measurement.rs:16-29). */
+int spz_prob0(spz_state_t h, uint32_t target, double* prob0);
+
+/* qubit_expectation_value(&State, target) = 2 prob0 - 1 (core.rs:198-219). */
+int spz_qubit_expectation_value(spz_state_t h, uint32_t target, double* out);
+
+/* xyz_expectation_value(observable, &State, targets) (core.rs:222-264).
+ * observable is 'x', 'y' or 'z'; out[i] = Re<psi|O_{targets[i]}|psi>. */
+int spz_xyz_expectation_value(spz_state_t h, char observable, const uint32_t* targets,
+                              uint32_t ntargets, double* out);
+
+/* A Pauli string coeff * X^x_mask Z^z_mask with Y on bits set in both masks
+ * (Y = i X Z per qubit, the phase is accounted for). */
+typedef struct spz_pauli_term {
+  double coeff;
+  uint64_t x_mask;
+  uint64_t z_mask;
+} spz_pauli_term;
+
+/* <psi|H|psi> for H = sum of Pauli terms, in fused tile passes.  No reference
+ * counterpart as one call; the reference builds it from xyz_expectation_value
+ * (clone + apply + Re inner product, core.rs:222-264). */
+int spz_pauli_expectation(spz_state_t h, const spz_pauli_term* terms, size_t nterms, double* out);
+
+/* Norm squared sum |a_i|^2 (deterministic order). */
+int spz_norm_sqr(spz_state_t h, double* out);
+
+/* Sample basis-state outcomes.  For each uniform u[k] in [0,1) the outcome is
+ * the inverse of the cumulative distribution of |a_i|^2 in the library's fixed
+ * blocked summation order (bit-reproducible).  Serves reservoir_sampling /
+ * get_samples (core.rs:67-129, spynoza/src/lib.rs:393-400). */
+int spz_sample(spz_state_t h, const double* u, size_t nshots, uint64_t* out);
+
+/* ---------------------------------------------------------- differentiation */
+/* Adjoint differentiation of E(theta) = <psi(theta)|H|psi(theta)> with
+ * psi(theta) = ops applied to the handle's current state.  Parameterised ops
+ * are the rotation gates (P, RX, RY, RZ, and their controlled forms) whose
+ * index appears in param_index: param_index[j] = k means d/d(ops[k].gate.p[0])
+ * goes to grad[j].  On return the handle holds psi(theta), *energy = E, grad[j]
+ * = dE/dtheta_j.  Needs two extra state vectors of device memory.
+ * No reference counterpart (new form built on the gate path). */
+int spz_adjoint_gradient(spz_state_t h, const spz_op* ops, size_t nops,
+                         const uint32_t* param_index, size_t nparams,
+                         const spz_pauli_term* terms, size_t nterms, double* energy,
+                         double* grad);
+
+/* ------------------------------------------------------------------ probes */
+/* Measured FP64 FMA issue rate of the current device (FMA/s): the second
+ * roofline (beside HBM bandwidth) that bounds dense FP64 gate kernels. */
+int spz_probe_fp64_fma_rate(double* fma_per_s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SPINOZA_GB300_H */

@@ -1,0 +1,187 @@
+"""ORACLE — test infrastructure only.
+
+ctypes wrapper around oracle/_build/liboracle.so, the CPU restatement of the
+reference's (QuState/spinoza v0.5.1) gate-application path.  Used only by
+tests/, __graft_entry__.smoke() and bench.py's CPU-baseline / reference arm, as
+the checker.  The product (spinoza_gb300/) never imports this package.
+
+Each function operates on numpy arrays (reals, imags) in place, like the
+reference's functions on `&mut State`.
+"""
+from __future__ import annotations
+
+import ctypes
+from ctypes import POINTER, byref, c_char, c_double, c_int, c_uint8, c_uint32, c_uint64, c_void_p
+from pathlib import Path
+from typing import Iterable, Optional, Sequence
+
+import numpy as np
+
+from . import build as _build
+
+H, M, X, Y, Z, P, RX, RY, RZ, SWAP, U, UNITARY, BITFLIP = range(13)
+
+
+class Gate(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int32), ("q0", c_uint32), ("q1", c_uint32), ("pad", c_uint32),
+                ("p", c_double * 3)]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build()
+        L = ctypes.CDLL(str(path))
+        v, d = c_void_p, c_double
+        sig = {
+            "orc_apply": [c_int, v, v, POINTER(Gate), c_int],
+            "orc_c_apply": [c_int, v, v, POINTER(Gate), c_int, c_int],
+            "orc_cc_apply": [c_int, v, v, POINTER(Gate), c_int, c_int, c_int],
+            "orc_mc_apply": [c_int, v, v, POINTER(Gate), c_uint64, c_uint64, c_int],
+            "orc_execute": [c_int, v, v, v, c_uint64, POINTER(c_uint64), POINTER(c_uint64)],
+            "orc_measure_qubit": [c_int, v, v, c_int, c_int, c_int, d, POINTER(c_uint8), POINTER(d)],
+            "orc_prob0": [c_int, v, v, c_int],
+            "orc_qubit_expectation_value": [c_int, v, v, c_int],
+            "orc_xyz_expectation_value": [c_int, v, v, c_char, v, c_uint32, v],
+            "orc_pauli_expectation": [c_int, v, v, v, c_uint64, POINTER(d)],
+            "orc_iqft": [c_int, v, v, v, c_uint32],
+            "orc_sample": [c_int, v, v, v, c_uint64, v],
+            "orc_stream_u64": [c_uint64, c_uint64],
+            "orc_stream_uniform": [c_uint64, c_uint64],
+            "orc_fill_uniform": [c_int, v, v, c_uint64],
+            "orc_num_threads": [],
+        }
+        res = {"orc_prob0": d, "orc_qubit_expectation_value": d, "orc_stream_u64": c_uint64,
+               "orc_stream_uniform": d, "orc_fill_uniform": None, "orc_num_threads": c_int}
+        for name, args in sig.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res.get(name, c_int)
+        _lib = L
+    return _lib
+
+
+def _p(a: np.ndarray) -> c_void_p:
+    assert a.flags.c_contiguous
+    return c_void_p(a.ctypes.data)
+
+
+def _n(re: np.ndarray) -> int:
+    n = int(re.size).bit_length() - 1
+    assert re.size == 1 << n and re.dtype == np.float64
+    return n
+
+
+class OracleError(RuntimeError):
+    pass
+
+
+def _check(rc: int) -> None:
+    if rc != 0:
+        raise OracleError(f"oracle status {rc}")
+
+
+def gate(kind: int, params: Sequence[float] = (), q0: int = 0, q1: int = 0) -> Gate:
+    g = Gate()
+    g.kind, g.q0, g.q1 = kind, q0, q1
+    for i, val in enumerate(params):
+        g.p[i] = float(val)
+    return g
+
+
+def zero_state(n: int) -> tuple[np.ndarray, np.ndarray]:
+    """State::new(n) (core.rs:32-42)."""
+    re = np.zeros(1 << n)
+    re[0] = 1.0
+    return re, np.zeros(1 << n)
+
+
+def apply(g: Gate, re: np.ndarray, im: np.ndarray, target: int) -> None:
+    _check(lib().orc_apply(_n(re), _p(re), _p(im), byref(g), target))
+
+
+def c_apply(g: Gate, re, im, control: int, target: int) -> None:
+    _check(lib().orc_c_apply(_n(re), _p(re), _p(im), byref(g), control, target))
+
+
+def cc_apply(g: Gate, re, im, c0: int, c1: int, target: int) -> None:
+    _check(lib().orc_cc_apply(_n(re), _p(re), _p(im), byref(g), c0, c1, target))
+
+
+def mc_apply(g: Gate, re, im, controls: Iterable[int], zeros: Optional[Iterable[int]], target: int) -> None:
+    cm = 0
+    for c in controls:
+        cm |= 1 << c
+    zm = 0
+    for z in zeros or ():
+        zm |= 1 << z
+    _check(lib().orc_mc_apply(_n(re), _p(re), _p(im), byref(g), cm, zm, target))
+
+
+def execute(ops: np.ndarray, re, im, measured: int = 0, values: int = 0) -> tuple[int, int]:
+    """QuantumCircuit::execute on an op array with the product's spz_op layout."""
+    m, v = c_uint64(measured), c_uint64(values)
+    ops = np.ascontiguousarray(ops)
+    _check(lib().orc_execute(_n(re), _p(re), _p(im), _p(ops), len(ops), byref(m), byref(v)))
+    return m.value, v.value
+
+
+def measure_qubit(re, im, target: int, reset: bool, forced: Optional[int] = None, u: float = 0.0) -> tuple[int, float]:
+    out, p0 = c_uint8(), c_double()
+    _check(lib().orc_measure_qubit(_n(re), _p(re), _p(im), target, int(reset), -1 if forced is None else forced,
+                                   u, byref(out), byref(p0)))
+    return out.value, p0.value
+
+
+def prob0(re, im, target: int) -> float:
+    return lib().orc_prob0(_n(re), _p(re), _p(im), target)
+
+
+def qubit_expectation_value(re, im, target: int) -> float:
+    return lib().orc_qubit_expectation_value(_n(re), _p(re), _p(im), target)
+
+
+def xyz_expectation_value(obs: str, re, im, targets: Sequence[int]) -> list[float]:
+    t = np.ascontiguousarray(np.array(targets, dtype=np.uint32))
+    out = np.empty(len(t))
+    _check(lib().orc_xyz_expectation_value(_n(re), _p(re), _p(im), obs.encode(), _p(t), len(t), _p(out)))
+    return out.tolist()
+
+
+def pauli_expectation(re, im, terms: np.ndarray) -> float:
+    terms = np.ascontiguousarray(terms)
+    out = c_double()
+    _check(lib().orc_pauli_expectation(_n(re), _p(re), _p(im), _p(terms), len(terms), byref(out)))
+    return out.value
+
+
+def iqft(re, im, targets: Sequence[int]) -> None:
+    t = np.ascontiguousarray(np.array(targets, dtype=np.uint32))
+    _check(lib().orc_iqft(_n(re), _p(re), _p(im), _p(t), len(t)))
+
+
+def sample(re, im, u: np.ndarray) -> np.ndarray:
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    out = np.empty(u.size, dtype=np.uint64)
+    _check(lib().orc_sample(_n(re), _p(re), _p(im), _p(u), u.size, _p(out)))
+    return out
+
+
+def uniform_state(n: int, seed: int) -> tuple[np.ndarray, np.ndarray]:
+    re, im = np.empty(1 << n), np.empty(1 << n)
+    lib().orc_fill_uniform(n, _p(re), _p(im), seed)
+    return re, im
+
+
+def stream_uniform(seed: int, i: int) -> float:
+    return lib().orc_stream_uniform(seed, i)
+
+
+def num_threads() -> int:
+    return lib().orc_num_threads()
+
+
+_ = Path

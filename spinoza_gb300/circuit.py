@@ -1,0 +1,275 @@
+"""Circuit builder and executor (spinoza/src/circuit.rs).
+
+Builders append ``QuantumTransformation``s; ``execute`` drains them into one
+flat op list and hands it to the device executor (spz_circuit_execute), which
+fuses runs of gates into shared-memory tile passes.
+"""
+from __future__ import annotations
+
+import math
+from ctypes import byref
+from typing import Iterable, List, Optional, Sequence, Set
+
+import numpy as np
+
+from . import _native as nat
+from . import rng
+from .core import State
+from .gates import Gate, next_noise_draw
+
+PI = math.pi
+
+
+class QuantumRegister:
+    """A list of qubit indices (circuit.rs:13-51)."""
+
+    def __init__(self, size: int):
+        if size <= 0:
+            raise nat.InvalidArgument(nat.SPZ_ERR_INVALID_ARGUMENT, "register size must be > 0 (circuit.rs:29)")
+        self.qubits = list(range(size))
+
+    def __getitem__(self, i: int) -> int:
+        return self.qubits[i]
+
+    def __len__(self) -> int:
+        return len(self.qubits)
+
+    def len(self) -> int:
+        return len(self.qubits)
+
+    def update_shift(self, shift: int) -> None:
+        self.qubits = [q + shift for q in self.qubits]
+
+    def get_shift(self) -> int:
+        return self.qubits[0]
+
+
+class Controls:
+    """None / Single / Ones / Mixed (circuit.rs:53-109)."""
+
+    NONE, SINGLE, ONES, MIXED = nat.CONTROLS_NONE, nat.CONTROLS_SINGLE, nat.CONTROLS_ONES, nat.CONTROLS_MIXED
+
+    __slots__ = ("kind", "controls", "zeros")
+
+    def __init__(self, kind: int, controls: Sequence[int] = (), zeros: Optional[Iterable[int]] = None):
+        self.kind = kind
+        self.controls = [int(c) for c in controls]
+        self.zeros: Set[int] = set(int(z) for z in zeros) if zeros else set()
+
+    @classmethod
+    def none(cls) -> "Controls":
+        return cls(cls.NONE)
+
+    @classmethod
+    def single(cls, c: int) -> "Controls":
+        return cls(cls.SINGLE, [c])
+
+    @classmethod
+    def ones(cls, cs: Sequence[int]) -> "Controls":
+        return cls(cls.ONES, cs)
+
+    @classmethod
+    def mixed(cls, controls: Sequence[int], zeros: Iterable[int]) -> "Controls":
+        return cls(cls.MIXED, controls, zeros)
+
+    @classmethod
+    def from_(cls, controls: Sequence[int], zeros: Optional[Set[int]]) -> "Controls":  # circuit.rs:71-84
+        if zeros:
+            return cls.mixed(controls, zeros)
+        if not controls:
+            return cls.none()
+        if len(controls) == 1:
+            return cls.single(controls[0])
+        return cls.ones(controls)
+
+    def unpack(self):  # circuit.rs:86-93
+        return list(self.controls), set(self.zeros)
+
+    def new_with_control(self, control: int, shift: int) -> "Controls":  # circuit.rs:95-105
+        controls, zeros = self.unpack()
+        controls = [c + shift for c in controls] + [control]
+        if not zeros:
+            return Controls.from_(controls, None)
+        return Controls.from_(controls, {z + shift for z in zeros})
+
+    def __repr__(self) -> str:
+        return f"Controls(kind={self.kind}, controls={self.controls}, zeros={sorted(self.zeros)})"
+
+
+class QuantumTransformation:
+    """gate + target + controls (circuit.rs:111-120)."""
+
+    __slots__ = ("gate", "target", "controls")
+
+    def __init__(self, gate: Gate, target: int, controls: Optional[Controls] = None):
+        self.gate = gate
+        self.target = int(target)
+        self.controls = controls if controls is not None else Controls.none()
+
+
+class QubitTracker:
+    """Measured qubits and their values (circuit.rs:122-164)."""
+
+    def __init__(self):
+        self.c = nat.spz_tracker(0, 0)
+
+    def is_qubit_measured(self, q: int) -> bool:
+        return bool((self.c.measured >> q) & 1)
+
+    def get_qubit_measured_val(self, q: int) -> Optional[int]:
+        return int((self.c.values >> q) & 1) if self.is_qubit_measured(q) else None
+
+
+def _ops_array(transformations: Sequence[QuantumTransformation], draws) -> np.ndarray:
+    ops = np.zeros(len(transformations), dtype=nat.OP_DTYPE)
+    for i, tr in enumerate(transformations):
+        g = tr.gate
+        if g.kind == nat.UNITARY:
+            raise nat.Unsupported(nat.SPZ_ERR_UNSUPPORTED, "dense Unitary transformations are not on this path")
+        p = list(g.params)
+        if g.kind == nat.M:
+            p[0] = draws()
+        elif g.kind == nat.BITFLIP and math.isnan(p[1]):
+            p[1] = next_noise_draw()
+        cmask = 0
+        for c in tr.controls.controls:
+            cmask |= 1 << c
+        zmask = 0
+        for z in tr.controls.zeros:
+            zmask |= 1 << z
+        ops[i] = ((g.kind, g.qubits[0], g.qubits[1], 0, p), tr.target, tr.controls.kind, cmask, zmask)
+    return ops
+
+
+class QuantumCircuit:
+    """A circuit over one or more registers (circuit.rs:166-601).
+
+    Keyword-only extensions: ``seed`` seeds the stream that resolves
+    measurement outcomes inside execute(); ``fused=False`` runs one kernel per
+    gate (the plain per-gate path)."""
+
+    def __init__(self, *registers: QuantumRegister, seed: int = 0, fused: bool = True, state: Optional[State] = None):
+        bits = 0
+        sizes = []
+        for r in registers:  # circuit.rs:181-198
+            r.update_shift(bits)
+            sizes.append(len(r))
+            bits += len(r)
+        self.transformations: List[QuantumTransformation] = []
+        self.quantum_registers_info = sizes
+        self.state = state if state is not None else State(bits)
+        self.qubit_tracker = QubitTracker()
+        self.fused = fused
+        self.last_stats = nat.spz_exec_stats()
+        self._seed = int(seed)
+        self._draw_index = 0
+
+    @classmethod
+    def from_state(cls, state: State, **kw) -> "QuantumCircuit":
+        qc = cls(state=state, **kw)
+        return qc
+
+    def get_statevector(self) -> State:
+        return self.state
+
+    def inverse(self) -> None:  # circuit.rs:206-211
+        self.transformations.reverse()
+        for tr in self.transformations:
+            tr.gate = tr.gate.inverse()
+
+    def add(self, transformation: QuantumTransformation) -> None:
+        self.transformations.append(transformation)
+
+    def _add(self, gate: Gate, target: int, controls: Optional[Controls] = None) -> None:
+        self.add(QuantumTransformation(gate, target, controls))
+
+    # builders (circuit.rs:214-445)
+    def measure(self, target: int) -> None: self._add(Gate.M, target)
+    def swap(self, t0: int, t1: int) -> None: self._add(Gate.SWAP(t0, t1), 0)
+    def x(self, target: int) -> None: self._add(Gate.X, target)
+    def y(self, target: int) -> None: self._add(Gate.Y, target)
+    def z(self, target: int) -> None: self._add(Gate.Z, target)
+    def h(self, target: int) -> None: self._add(Gate.H, target)
+    def p(self, angle: float, target: int) -> None: self._add(Gate.P(angle), target)
+    def rx(self, angle: float, target: int) -> None: self._add(Gate.RX(angle), target)
+    def ry(self, angle: float, target: int) -> None: self._add(Gate.RY(angle), target)
+    def rz(self, angle: float, target: int) -> None: self._add(Gate.RZ(angle), target)
+    def u(self, theta: float, phi: float, lam: float, target: int) -> None: self._add(Gate.U(theta, phi, lam), target)
+    def cx(self, control: int, target: int) -> None: self._add(Gate.X, target, Controls.single(control))
+    def ccx(self, c1: int, c2: int, target: int) -> None: self._add(Gate.X, target, Controls.ones([c1, c2]))
+    def ch(self, control: int, target: int) -> None: self._add(Gate.H, target, Controls.single(control))
+    def cy(self, control: int, target: int) -> None: self._add(Gate.Y, target, Controls.single(control))
+    def cz(self, control: int, target: int) -> None: self._add(Gate.Z, target, Controls.single(control))
+    def cp(self, angle: float, control: int, target: int) -> None: self._add(Gate.P(angle), target, Controls.single(control))
+    def crx(self, angle: float, control: int, target: int) -> None: self._add(Gate.RX(angle), target, Controls.single(control))
+    def cry(self, angle: float, control: int, target: int) -> None: self._add(Gate.RY(angle), target, Controls.single(control))
+    def crz(self, angle: float, control: int, target: int) -> None: self._add(Gate.RZ(angle), target, Controls.single(control))
+
+    def cu(self, theta: float, phi: float, lam: float, control: int, target: int) -> None:
+        self._add(Gate.U(theta, phi, lam), target, Controls.single(control))
+
+    def bit_flip_noise(self, prob: float, target: int) -> None:
+        self._add(Gate.BitFlipNoise(prob), target)
+
+    def iqft(self, targets: Sequence[int]) -> None:  # circuit.rs:438-445
+        for j in range(len(targets) - 1, -1, -1):
+            self.h(targets[j])
+            for k in range(j - 1, -1, -1):
+                self.cp(-PI / 2.0 ** (j - k), targets[j], targets[k])
+
+    def append(self, circuit: "QuantumCircuit", reg: QuantumRegister) -> None:  # circuit.rs:448-460
+        if len(reg) != sum(circuit.quantum_registers_info):
+            raise nat.InvalidArgument(nat.SPZ_ERR_INVALID_ARGUMENT, "register size mismatch (circuit.rs:449)")
+        for tr in circuit.transformations:
+            self.add(QuantumTransformation(tr.gate, reg.get_shift() + tr.target, tr.controls))
+
+    def c_append(self, circuit: "QuantumCircuit", c: int, reg: QuantumRegister) -> None:  # circuit.rs:463-477
+        if reg.get_shift() <= c < reg.get_shift() + len(reg):
+            raise nat.InvalidArgument(nat.SPZ_ERR_INVALID_ARGUMENT, "control inside the register (circuit.rs:464)")
+        for tr in circuit.transformations:
+            self.add(QuantumTransformation(tr.gate, reg.get_shift() + tr.target,
+                                           tr.controls.new_with_control(c, reg.get_shift())))
+
+    def mc_append(self, circuit: "QuantumCircuit", controls: Sequence[int], reg: QuantumRegister) -> None:
+        """circuit.rs:480-511 (appends the circuit once per control, as the reference does)."""
+        if len(set(controls)) != len(controls):
+            raise nat.InvalidArgument(nat.SPZ_ERR_INVALID_ARGUMENT, "duplicate controls (circuit.rs:488)")
+        lo, hi = reg.get_shift(), reg.get_shift() + len(reg)
+        for c in controls:
+            if lo <= c < hi:
+                raise nat.InvalidArgument(nat.SPZ_ERR_INVALID_ARGUMENT,
+                                          f"control {c} should not be in: Range(start: {lo} end: {hi})")
+        for control in controls:
+            for tr in circuit.transformations:
+                self.add(QuantumTransformation(tr.gate, reg.get_shift() + tr.target,
+                                               tr.controls.new_with_control(control, reg.get_shift())))
+
+    # execution
+    def _next_draw(self) -> float:
+        u = float(rng.uniforms(self._seed, 1, self._draw_index)[0])
+        self._draw_index += 1
+        return u
+
+    def ops(self) -> np.ndarray:
+        """The pending transformations as a C-ABI op array (draws resolved)."""
+        return _ops_array(self.transformations, self._next_draw)
+
+    def execute(self) -> None:  # circuit.rs:552-600 (drains the transformations)
+        ops = self.ops()
+        self.transformations = []
+        self.execute_ops(ops)
+
+    def execute_ops(self, ops: np.ndarray) -> None:
+        ops = np.ascontiguousarray(ops, dtype=nat.OP_DTYPE)
+        flags = nat.EXEC_DEFAULT if self.fused else nat.EXEC_UNFUSED
+        nat.check(nat.lib().spz_circuit_execute(self.state.handle, nat.ptr(ops), len(ops),
+                                                byref(self.qubit_tracker.c), flags, byref(self.last_stats)))
+
+
+def plan_stats(n: int, ops: np.ndarray, fused: bool = True) -> dict:
+    """How the executor would fuse `ops` on n qubits (host only, no GPU)."""
+    st = nat.spz_exec_stats()
+    ops = np.ascontiguousarray(ops, dtype=nat.OP_DTYPE)
+    flags = nat.EXEC_DEFAULT if fused else nat.EXEC_UNFUSED
+    nat.check(nat.lib().spz_plan_stats(int(n), nat.ptr(ops), len(ops), flags, byref(st)))
+    return {f: getattr(st, f) for f, _ in nat.spz_exec_stats._fields_}

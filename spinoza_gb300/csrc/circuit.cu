@@ -1,0 +1,646 @@
+// Circuit executor: QuantumCircuit::execute (spinoza/src/circuit.rs:552-600)
+// and iqft (spinoza/src/core.rs:184-191).
+//
+// The reference makes one full pass over the state per gate.  Here a host-side
+// planner groups gates into passes over shared-memory tiles: a pass fixes a set
+// L of k "local" qubits (always including the lowest qubits, so every tile row is
+// a contiguous, coalesced run of amplitudes); each thread block loads a tile of
+// 2^k amplitudes (all values of the local bits, for one value of the other
+// bits) into shared memory, applies every gate of the pass whose target(s) lie
+// in L — controls and diagonal gates may sit on any qubit — and writes the tile
+// back.  A run of gates costs one HBM read and one write of the state.
+//
+// Exactness: each gate's per-pair arithmetic is the plain kernel's (the
+// reference's own operations).  The planner keeps program order except where a
+// swap of two gates is bit-exact: they commute on disjoint non-diagonal qubits
+// and one of them only moves or negates amplitudes (X, Y, Z, SWAP and their
+// controlled forms).  So a fused run is bit-identical to the sequential one.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "common.cuh"
+#include "gate_math.cuh"
+
+namespace spz {
+
+int measure_qubit(spz_state_t h, uint32_t target, int reset, int forced, double u, uint8_t* outcome,
+                  double* prob0_out);
+int apply_controlled(spz_state_t h, const spz_gate* gate, uint32_t target, uint64_t ones, uint64_t zeros);
+
+constexpr int kTileMaxK = 12;     // 2^12 amplitudes x 16 B = 64 KiB of shared memory
+constexpr int kTileLowBits = 3;   // qubits 0..2 always local: 64-byte contiguous rows
+constexpr int kTileThreads = 512;
+
+enum TileMode { TM_PAIR = 0, TM_DIAG_LOCAL = 1, TM_DIAG_GLOBAL = 2, TM_SWAP = 3 };
+
+struct TileGate {
+  int32_t kind;
+  int32_t mode;
+  uint32_t tbit;    // local bit of the target (SWAP: first qubit)
+  uint32_t tbit2;   // SWAP: local bit of the second qubit
+  uint32_t l_ones;  // local bits that must be 1 (controls; plus the target for Z/P on s1)
+  int32_t npos;     // number of local positions inserted by the enumeration
+  uint8_t pos[16];  // sorted local bit positions inserted as zeros
+  uint64_t g_ones;  // non-local bits the tile base must have set
+  uint64_t g_zeros; // non-local bits the tile base must have clear
+  uint64_t g_tbit;  // TM_DIAG_GLOBAL: the non-local target bit
+  Coef c;
+};
+
+struct PassArgs {
+  double* re;
+  double* im;
+  uint64_t ntiles;
+  const TileGate* gates;
+  int ngates;
+  int k;            // local qubits
+  int c;            // low contiguous local qubits (0..c-1)
+  int nhigh;        // k - c
+  uint8_t lpos[kTileMaxK];  // sorted local qubits
+};
+
+// ------------------------------------------------------------ device side
+template <int KIND>
+__device__ __forceinline__ void tile_pair(const TileGate& g, double* sre, double* sim, uint32_t npairs) {
+  for (uint32_t m = threadIdx.x; m < npairs; m += blockDim.x) {
+    const uint32_t s0 = (uint32_t)deposit(m, g.pos, g.npos) | g.l_ones;
+    const uint32_t s1 = s0 | g.tbit;
+    double a = sre[s0], b = sim[s0], c = sre[s1], d = sim[s1];
+    gate_pair<KIND>(g.c, a, b, c, d);
+    sre[s0] = a; sim[s0] = b; sre[s1] = c; sim[s1] = d;
+  }
+}
+
+template <int KIND>
+__device__ __forceinline__ void tile_diag(const TileGate& g, double* sre, double* sim, uint32_t nelem, int global_one) {
+  for (uint32_t m = threadIdx.x; m < nelem; m += blockDim.x) {
+    const uint32_t e = (uint32_t)deposit(m, g.pos, g.npos) | g.l_ones;
+    const bool one = global_one >= 0 ? global_one != 0 : (e & g.tbit) != 0;
+    double r = sre[e], i = sim[e];
+    gate_diag<KIND>(g.c, one, r, i);
+    sre[e] = r; sim[e] = i;
+  }
+}
+
+__global__ void __launch_bounds__(kTileThreads) tile_kernel(PassArgs A) {
+  extern __shared__ double smem[];
+  const int K = A.k;
+  const uint32_t T = 1u << K;
+  double* sre = smem;
+  double* sim = smem + T;
+  uint64_t* rowoff = reinterpret_cast<uint64_t*>(smem + 2 * T);
+  const uint32_t nrows = 1u << A.nhigh;
+  const uint32_t cmask = (1u << A.c) - 1;
+  // Row offsets: scatter of the high local bits, the same for every tile.
+  for (uint32_t r = threadIdx.x; r < nrows; r += blockDim.x) {
+    uint64_t off = 0;
+    for (int j = 0; j < A.nhigh; ++j)
+      if ((r >> j) & 1) off |= 1ull << A.lpos[A.c + j];
+    rowoff[r] = off;
+  }
+  __syncthreads();
+  for (uint64_t tile = blockIdx.x; tile < A.ntiles; tile += gridDim.x) {
+    const uint64_t base = deposit(tile, A.lpos, K);
+    // load (pairs of consecutive amplitudes: c >= 1)
+    for (uint32_t e2 = threadIdx.x; e2 < T / 2; e2 += blockDim.x) {
+      const uint32_t e = 2 * e2;
+      const uint64_t gi = base | rowoff[e >> A.c] | (e & cmask);
+      const double2 r = *reinterpret_cast<const double2*>(A.re + gi);
+      const double2 m = *reinterpret_cast<const double2*>(A.im + gi);
+      *reinterpret_cast<double2*>(sre + e) = r;
+      *reinterpret_cast<double2*>(sim + e) = m;
+    }
+    __syncthreads();
+    for (int gi = 0; gi < A.ngates; ++gi) {
+      const TileGate& g = A.gates[gi];
+      if ((base & g.g_ones) != g.g_ones || (base & g.g_zeros) != 0) continue;  // uniform per tile
+      const uint32_t nw = T >> g.npos;
+      switch (g.mode) {
+        case TM_PAIR:
+          switch (g.kind) {
+            case SPZ_GATE_H: tile_pair<SPZ_GATE_H>(g, sre, sim, nw); break;
+            case SPZ_GATE_X: tile_pair<SPZ_GATE_X>(g, sre, sim, nw); break;
+            case SPZ_GATE_Y: tile_pair<SPZ_GATE_Y>(g, sre, sim, nw); break;
+            case SPZ_GATE_RX: tile_pair<SPZ_GATE_RX>(g, sre, sim, nw); break;
+            case SPZ_GATE_RY: tile_pair<SPZ_GATE_RY>(g, sre, sim, nw); break;
+            default: tile_pair<SPZ_GATE_U>(g, sre, sim, nw); break;
+          }
+          break;
+        case TM_DIAG_LOCAL:
+        case TM_DIAG_GLOBAL: {
+          int gone = -1;
+          if (g.mode == TM_DIAG_GLOBAL) {
+            gone = (base & g.g_tbit) ? 1 : 0;
+            if (!gone && g.kind != SPZ_GATE_RZ) break;  // Z / P act on the 1 half only
+          }
+          switch (g.kind) {
+            case SPZ_GATE_Z: tile_diag<SPZ_GATE_Z>(g, sre, sim, nw, gone); break;
+            case SPZ_GATE_P: tile_diag<SPZ_GATE_P>(g, sre, sim, nw, gone); break;
+            default: tile_diag<SPZ_GATE_RZ>(g, sre, sim, nw, gone); break;
+          }
+          break;
+        }
+        default: {  // TM_SWAP
+          for (uint32_t m = threadIdx.x; m < nw; m += blockDim.x) {
+            const uint32_t b0 = (uint32_t)deposit(m, g.pos, g.npos) | g.l_ones;
+            const uint32_t i = b0 | g.tbit2, j = b0 | g.tbit;
+            const double r = sre[i], q = sim[i];
+            sre[i] = sre[j]; sim[i] = sim[j];
+            sre[j] = r; sim[j] = q;
+          }
+        }
+      }
+      __syncthreads();
+    }
+    // store
+    for (uint32_t e2 = threadIdx.x; e2 < T / 2; e2 += blockDim.x) {
+      const uint32_t e = 2 * e2;
+      const uint64_t gi = base | rowoff[e >> A.c] | (e & cmask);
+      *reinterpret_cast<double2*>(A.re + gi) = *reinterpret_cast<const double2*>(sre + e);
+      *reinterpret_cast<double2*>(A.im + gi) = *reinterpret_cast<const double2*>(sim + e);
+    }
+    __syncthreads();
+  }
+}
+
+// ------------------------------------------------------------ planner
+namespace {
+
+inline bool arithmetic_free(int kind) {
+  return kind == SPZ_GATE_X || kind == SPZ_GATE_Y || kind == SPZ_GATE_Z || kind == SPZ_GATE_SWAP;
+}
+
+// Qubits a gate acts on non-diagonally (targets of pair gates, SWAP qubits)
+// and diagonally only (controls, and all qubits of diagonal gates).
+inline uint64_t nd_mask(const GateApp& g) {
+  if (g.kind == SPZ_GATE_SWAP) return (1ull << g.target) | (1ull << g.target2);
+  if (is_diagonal(g.kind)) return 0;
+  return 1ull << g.target;
+}
+inline uint64_t d_mask(const GateApp& g) {
+  uint64_t m = g.ones | g.zeros;
+  if (is_diagonal(g.kind)) m |= 1ull << g.target;
+  return m;
+}
+
+struct PlannedPass {
+  std::vector<int> local;        // sorted local qubits
+  std::vector<GateApp> gates;
+};
+
+// Greedy planner: see the file comment.  `k` local qubits per pass, the low
+// `c` qubits always local.
+std::vector<PlannedPass> plan(const std::vector<GateApp>& gates, uint32_t n, int k, int c) {
+  std::vector<PlannedPass> passes;
+  std::vector<GateApp> remaining = gates;
+  const uint64_t low = c >= 64 ? ~0ull : ((1ull << c) - 1);
+  while (!remaining.empty()) {
+    PlannedPass P;
+    uint64_t L = low;
+    int nl = __builtin_popcountll(L);
+    std::vector<GateApp> deferred;
+    uint64_t def_nd = 0, def_d = 0;
+    bool def_arith = false;
+    const size_t lookahead = 4096;
+    size_t i = 0;
+    for (; i < remaining.size(); ++i) {
+      const GateApp& g = remaining[i];
+      if (deferred.size() > lookahead) break;
+      const uint64_t nd = nd_mask(g), d = d_mask(g);
+      const bool commutes = (nd & (def_nd | def_d)) == 0 && (d & def_nd) == 0;
+      const bool exact_ok = arithmetic_free(g.kind) || !def_arith;
+      bool take = false;
+      if (deferred.empty() || (commutes && exact_ok)) {
+        const uint64_t need = nd & ~L;
+        const int add = __builtin_popcountll(need);
+        if (nl + add <= k) {
+          L |= need;
+          nl += add;
+          take = true;
+        }
+      }
+      if (take) {
+        P.gates.push_back(g);
+      } else {
+        deferred.push_back(g);
+        def_nd |= nd;
+        def_d |= d;
+        def_arith |= !arithmetic_free(g.kind);
+      }
+    }
+    for (; i < remaining.size(); ++i) deferred.push_back(remaining[i]);
+    if (P.gates.empty()) {  // cannot happen for k >= c + 2; keep progress regardless
+      P.gates.push_back(deferred.front());
+      deferred.erase(deferred.begin());
+      L |= nd_mask(P.gates[0]);
+    }
+    for (int q = 0; q < (int)n; ++q)
+      if ((L >> q) & 1) P.local.push_back(q);
+    passes.push_back(std::move(P));
+    remaining.swap(deferred);
+  }
+  return passes;
+}
+
+// Build the device description of a gate inside a pass with local qubits `L`.
+TileGate tile_gate(const GateApp& g, const std::vector<int>& local) {
+  int where[64];
+  for (int q = 0; q < 64; ++q) where[q] = -1;
+  for (size_t j = 0; j < local.size(); ++j) where[local[j]] = (int)j;
+  TileGate t{};
+  t.kind = g.kind;
+  t.c = g.c;
+  uint32_t l_ones = 0, l_zeros = 0;
+  for (int q = 0; q < 64; ++q) {
+    const uint64_t b = 1ull << q;
+    if (g.ones & b) {
+      if (where[q] >= 0) l_ones |= 1u << where[q]; else t.g_ones |= b;
+    }
+    if (g.zeros & b) {
+      if (where[q] >= 0) l_zeros |= 1u << where[q]; else t.g_zeros |= b;
+    }
+  }
+  uint32_t special = l_ones | l_zeros;
+  if (g.kind == SPZ_GATE_SWAP) {
+    t.mode = TM_SWAP;
+    t.tbit = 1u << where[g.target];
+    t.tbit2 = 1u << where[g.target2];
+    special |= t.tbit | t.tbit2;
+    t.l_ones = l_ones;
+  } else if (is_diagonal(g.kind)) {
+    if (where[g.target] >= 0) {
+      t.mode = TM_DIAG_LOCAL;
+      t.tbit = 1u << where[g.target];
+      if (g.kind != SPZ_GATE_RZ) {  // Z and P touch the target-1 half only
+        special |= t.tbit;
+        l_ones |= t.tbit;
+      }
+    } else {
+      t.mode = TM_DIAG_GLOBAL;
+      t.g_tbit = 1ull << g.target;
+    }
+    t.l_ones = l_ones;
+  } else {
+    t.mode = TM_PAIR;
+    t.tbit = 1u << where[g.target];
+    special |= t.tbit;
+    t.l_ones = l_ones;
+  }
+  t.npos = 0;
+  for (int j = 0; j < 32; ++j)
+    if ((special >> j) & 1) t.pos[t.npos++] = (uint8_t)j;
+  return t;
+}
+
+struct Segment {
+  std::vector<GateApp> gates;
+};
+
+}  // namespace
+
+namespace {
+
+// Optional per-pass device timing (SPZ_EXEC_TIME_PASSES): an event pair around
+// every launch on the handle's stream, summed after one synchronisation.
+struct PassTimer {
+  bool on = false;
+  cudaStream_t stream = nullptr;
+  std::vector<cudaEvent_t> ev;
+  std::vector<bool> tile;
+  int begin() {
+    if (!on) return SPZ_OK;
+    cudaEvent_t a, b;
+    SPZ_CUDA(cudaEventCreate(&a));
+    SPZ_CUDA(cudaEventCreate(&b));
+    ev.push_back(a);
+    ev.push_back(b);
+    SPZ_CUDA(cudaEventRecord(a, stream));
+    return SPZ_OK;
+  }
+  int end(bool is_tile) {
+    if (!on) return SPZ_OK;
+    SPZ_CUDA(cudaEventRecord(ev.back(), stream));
+    tile.push_back(is_tile);
+    return SPZ_OK;
+  }
+  int collect(spz_exec_stats* st) {
+    if (!on) return SPZ_OK;
+    int rc = SPZ_OK;
+    cudaError_t e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) rc = cuda_fail(e, "pass timing synchronisation");
+    for (size_t i = 0; i + 1 < ev.size(); i += 2) {
+      float ms = 0.f;
+      if (rc == SPZ_OK && i / 2 < tile.size() && cudaEventElapsedTime(&ms, ev[i], ev[i + 1]) == cudaSuccess && st)
+        (tile[i / 2] ? st->tile_ms : st->plain_ms) += ms;
+      cudaEventDestroy(ev[i]);
+      cudaEventDestroy(ev[i + 1]);
+    }
+    ev.clear();
+    tile.clear();
+    return rc;
+  }
+};
+
+}  // namespace
+
+// Run a list of already validated gate applications on h.
+int run_gates(spz_state_t h, const std::vector<GateApp>& gates, uint32_t flags, spz_exec_stats* st) {
+  if (gates.empty()) return SPZ_OK;
+  const uint32_t n = h->n;
+  PassTimer timer;
+  timer.on = (flags & SPZ_EXEC_TIME_PASSES) != 0;
+  timer.stream = h->stream;
+  if (flags & SPZ_EXEC_UNFUSED) {
+    for (const GateApp& g : gates) {
+      int rc = timer.begin();
+      if (!rc) rc = launch_gate(h, g);
+      if (!rc) rc = timer.end(false);
+      if (rc) {
+        timer.collect(nullptr);
+        return rc;
+      }
+      if (st) {
+        st->passes++;
+        st->bytes_moved += gate_algorithmic_bytes(n, g);
+      }
+    }
+    return timer.collect(st);
+  }
+  const int k = std::min<int>((int)n, kTileMaxK);
+  const int c = std::min<int>(kTileLowBits, k);
+  std::vector<PlannedPass> passes = plan(gates, n, k, c);
+  // Upload every tile gate of every fused pass in one copy.
+  std::vector<TileGate> all;
+  std::vector<size_t> offs;
+  for (const PlannedPass& P : passes) {
+    offs.push_back(all.size());
+    if (P.gates.size() > 1)
+      for (const GateApp& g : P.gates) all.push_back(tile_gate(g, P.local));
+  }
+  TileGate* dgates = nullptr;
+  if (!all.empty()) {
+    void* dscr;
+    const size_t bytes = all.size() * sizeof(TileGate);
+    int rc = ensure_dev_scratch(h, bytes, &dscr);
+    if (rc) return rc;
+    // From pageable memory: the runtime stages the bytes before returning, so
+    // `all` may go out of scope while the copy is still queued on the stream.
+    SPZ_CUDA(cudaMemcpyAsync(dscr, all.data(), bytes, cudaMemcpyHostToDevice, h->stream));
+    dgates = (TileGate*)dscr;
+  }
+  static bool attr_set = false;
+  if (!attr_set) {
+    SPZ_CUDA(cudaFuncSetAttribute(tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (2 << kTileMaxK) * 8 + (1 << kTileMaxK) * 8));
+    attr_set = true;
+  }
+  for (size_t p = 0; p < passes.size(); ++p) {
+    const PlannedPass& P = passes[p];
+    if (P.gates.size() == 1) {  // a lone gate: the plain kernel touches only what it needs
+      int rc = timer.begin();
+      if (!rc) rc = launch_gate(h, P.gates[0]);
+      if (!rc) rc = timer.end(false);
+      if (rc) {
+        timer.collect(nullptr);
+        return rc;
+      }
+      if (st) {
+        st->passes++;
+        st->bytes_moved += gate_algorithmic_bytes(n, P.gates[0]);
+      }
+      continue;
+    }
+    PassArgs A{};
+    A.re = h->re;
+    A.im = h->im;
+    A.k = (int)P.local.size();
+    A.c = c;
+    A.nhigh = A.k - c;
+    for (int j = 0; j < A.k; ++j) A.lpos[j] = (uint8_t)P.local[j];
+    A.ntiles = 1ull << (n - A.k);
+    A.gates = dgates + offs[p];
+    A.ngates = (int)P.gates.size();
+    const uint32_t T = 1u << A.k;
+    const size_t smem = 2 * T * sizeof(double) + (size_t)(1u << A.nhigh) * sizeof(uint64_t);
+    const int threads = (int)std::min<uint32_t>(kTileThreads, std::max<uint32_t>(32, T / 2));
+    const uint64_t blocks = std::min<uint64_t>(A.ntiles, (uint64_t)kNumSMs * 4);
+    int rc = timer.begin();
+    if (rc) {
+      timer.collect(nullptr);
+      return rc;
+    }
+    tile_kernel<<<(unsigned)blocks, threads, smem, h->stream>>>(A);
+    cudaError_t le = cudaGetLastError();
+    if (le != cudaSuccess) {
+      timer.collect(nullptr);
+      return cuda_fail(le, "tile_kernel");
+    }
+    rc = timer.end(true);
+    if (rc) {
+      timer.collect(nullptr);
+      return rc;
+    }
+    if (st) {
+      st->passes++;
+      st->tile_passes++;
+      st->bytes_moved += 32ull << n;
+    }
+  }
+  return timer.collect(st);
+}
+
+namespace {
+
+// Resolve one op of a circuit into zero or one GateApp (no M).
+int op_to_app(spz_state_t h, const spz_op& op, const spz_tracker& tr, bool* skip, GateApp* out) {
+  *skip = false;
+  spz_gate gate = op.gate;
+  uint64_t ones = 0, zeros = 0;
+  switch (op.controls_kind) {
+    case SPZ_CONTROLS_NONE:
+      break;
+    case SPZ_CONTROLS_SINGLE: {
+      if (op.controls == 0 || (op.controls & (op.controls - 1)) != 0)
+        return fail(SPZ_ERR_INVALID_ARGUMENT, "Single controls need exactly one control qubit");
+      const int c = __builtin_ctzll(op.controls);
+      if ((tr.measured >> c) & 1) {  // classical control (circuit.rs:570-578)
+        if (!((tr.values >> c) & 1)) {
+          *skip = true;
+          return SPZ_OK;
+        }
+      } else {
+        ones = op.controls;
+      }
+      break;
+    }
+    case SPZ_CONTROLS_ONES:
+      ones = op.controls;
+      break;
+    case SPZ_CONTROLS_MIXED:
+      if (op.zeros & ~op.controls) return fail(SPZ_ERR_INVALID_ARGUMENT, "zeros must be a subset of controls");
+      ones = op.controls & ~op.zeros;
+      zeros = op.zeros;
+      break;
+    default:
+      return fail(SPZ_ERR_INVALID_ARGUMENT, "unknown controls kind");
+  }
+  if (gate.kind == SPZ_GATE_BITFLIP) {  // gates.rs:1365-1374 with the draw in p[1]
+    if (!(gate.p[1] <= gate.p[0])) {
+      if (op.target >= h->n) return fail(SPZ_ERR_INVALID_ARGUMENT, "target qubit out of range");
+      *skip = true;
+      return SPZ_OK;
+    }
+    gate = spz_gate{};
+    gate.kind = SPZ_GATE_X;
+  }
+  return make_gate_app(h->n, gate, op.target, ones, zeros, out);
+}
+
+}  // namespace
+
+int execute(spz_state_t h, const spz_op* ops, size_t nops, spz_tracker* tracker, uint32_t flags,
+            spz_exec_stats* st) {
+  spz_tracker tr{};
+  if (tracker) tr = *tracker;
+  std::vector<GateApp> seg;
+  for (size_t i = 0; i < nops; ++i) {
+    const spz_op& op = ops[i];
+    if (op.gate.kind == SPZ_GATE_M) {  // circuit.rs:559-566: a barrier
+      if (op.controls_kind != SPZ_CONTROLS_NONE)
+        return fail(SPZ_ERR_UNSUPPORTED, "a measurement cannot be controlled");
+      if (op.target >= h->n) return fail(SPZ_ERR_INVALID_ARGUMENT, "target qubit out of range");
+      if (!((tr.measured >> op.target) & 1)) {
+        int rc = run_gates(h, seg, flags, st);
+        if (rc) return rc;
+        seg.clear();
+        uint8_t v = 0;
+        rc = measure_qubit(h, op.target, 1, -1, op.gate.p[0], &v, nullptr);
+        if (rc) return rc;
+        tr.measured |= 1ull << op.target;
+        tr.values = (tr.values & ~(1ull << op.target)) | ((uint64_t)v << op.target);
+        if (st) st->passes += 2;
+      }
+      continue;
+    }
+    bool skip;
+    GateApp a;
+    int rc = op_to_app(h, op, tr, &skip, &a);
+    if (rc) return rc;
+    if (skip) continue;
+    seg.push_back(a);
+    if (st) {
+      st->gates++;
+      st->algorithmic_bytes += gate_algorithmic_bytes(h->n, a);
+      st->fp64_ops += gate_fp64_ops(h->n, a);
+    }
+  }
+  int rc = run_gates(h, seg, flags, st);
+  if (rc) return rc;
+  if (tracker) *tracker = tr;
+  return SPZ_OK;
+}
+
+// Plan without executing (host only): fills the counters run_gates would.
+int plan_stats(uint32_t n, const spz_op* ops, size_t nops, uint32_t flags, spz_exec_stats* st) {
+  spz_state_s fake;
+  fake.n = n;
+  fake.N = 1ull << n;
+  spz_tracker tr{};
+  std::vector<GateApp> seg;
+  auto flush = [&]() {
+    if (seg.empty()) return;
+    if (flags & SPZ_EXEC_UNFUSED) {
+      for (const GateApp& g : seg) {
+        st->passes++;
+        st->bytes_moved += gate_algorithmic_bytes(n, g);
+      }
+    } else {
+      const int k = std::min<int>((int)n, kTileMaxK);
+      const int c = std::min<int>(kTileLowBits, k);
+      for (const PlannedPass& P : plan(seg, n, k, c)) {
+        st->passes++;
+        if (P.gates.size() > 1) {
+          st->tile_passes++;
+          st->bytes_moved += 32ull << n;
+        } else {
+          st->bytes_moved += gate_algorithmic_bytes(n, P.gates[0]);
+        }
+      }
+    }
+    seg.clear();
+  };
+  for (size_t i = 0; i < nops; ++i) {
+    const spz_op& op = ops[i];
+    if (op.gate.kind == SPZ_GATE_M) {
+      if (op.controls_kind != SPZ_CONTROLS_NONE) return fail(SPZ_ERR_UNSUPPORTED, "a measurement cannot be controlled");
+      if (op.target >= n) return fail(SPZ_ERR_INVALID_ARGUMENT, "target qubit out of range");
+      if (!((tr.measured >> op.target) & 1)) {
+        flush();
+        tr.measured |= 1ull << op.target;  // outcome unknown while planning: assume 0
+        st->passes += 2;
+      }
+      continue;
+    }
+    bool skip;
+    GateApp a;
+    int rc = op_to_app(&fake, op, tr, &skip, &a);
+    if (rc) return rc;
+    if (skip) continue;
+    seg.push_back(a);
+    st->gates++;
+    st->algorithmic_bytes += gate_algorithmic_bytes(n, a);
+    st->fp64_ops += gate_fp64_ops(n, a);
+  }
+  flush();
+  return SPZ_OK;
+}
+
+}  // namespace spz
+
+using namespace spz;
+
+extern "C" {
+
+int spz_circuit_execute(spz_state_t h, const spz_op* ops, size_t nops, spz_tracker* tracker, uint32_t flags,
+                        spz_exec_stats* stats) {
+  if (!h) return fail(SPZ_ERR_NULL, "handle is NULL");
+  if (nops && !ops) return fail(SPZ_ERR_NULL, "ops is NULL");
+  if (stats) std::memset(stats, 0, sizeof(*stats));
+  return execute(h, ops, nops, tracker, flags, stats);
+}
+
+int spz_plan_stats(uint32_t n, const spz_op* ops, size_t nops, uint32_t flags, spz_exec_stats* stats) {
+  if (!stats) return fail(SPZ_ERR_NULL, "stats is NULL");
+  if (nops && !ops) return fail(SPZ_ERR_NULL, "ops is NULL");
+  if (n == 0 || n > kMaxQubits) return fail(SPZ_ERR_INVALID_ARGUMENT, "n out of range");
+  std::memset(stats, 0, sizeof(*stats));
+  return plan_stats(n, ops, nops, flags, stats);
+}
+
+// core.rs:184-191: for j = len-1 .. 0: H(targets[j]); for k = j-1 .. 0:
+// CP(-pi / 2^(j-k)) with control targets[j], target targets[k].
+int spz_iqft(spz_state_t h, const uint32_t* targets, uint32_t ntargets) {
+  if (!h) return fail(SPZ_ERR_NULL, "handle is NULL");
+  if (ntargets && !targets) return fail(SPZ_ERR_NULL, "targets is NULL");
+  std::vector<spz_op> ops;
+  for (int64_t j = (int64_t)ntargets - 1; j >= 0; --j) {
+    spz_op op{};
+    op.gate.kind = SPZ_GATE_H;
+    op.target = targets[j];
+    ops.push_back(op);
+    for (int64_t k = j - 1; k >= 0; --k) {
+      spz_op cp{};
+      cp.gate.kind = SPZ_GATE_P;
+      cp.gate.p[0] = -3.14159265358979323846 / std::ldexp(1.0, (int)(j - k));
+      cp.target = targets[k];
+      cp.controls_kind = SPZ_CONTROLS_SINGLE;
+      if (targets[j] >= 64) return fail(SPZ_ERR_INVALID_ARGUMENT, "target qubit out of range");
+      cp.controls = 1ull << targets[j];
+      ops.push_back(cp);
+    }
+  }
+  return execute(h, ops.data(), ops.size(), nullptr, SPZ_EXEC_DEFAULT, nullptr);
+}
+
+}  // extern "C"

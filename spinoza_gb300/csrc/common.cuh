@@ -1,0 +1,142 @@
+// Shared definitions of the spinoza_gb300 CUDA library (sm_103a).
+//
+// State layout in HBM: two FP64 arrays reals[2^n], imags[2^n] (SoA), as
+// `State { reals, imags, n }` in spinoza/src/core.rs:20-27.  Amplitude index i
+// has bit q equal to the value of qubit q.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+
+#include "../../include/spinoza_gb300.h"
+
+namespace spz {
+
+constexpr int kMaxQubits = SPZ_MAX_QUBITS;
+constexpr int kNumSMs = 152;          // GB300: 2 dies x 76 SMs
+constexpr int kThreads = 256;
+
+// ------------------------------------------------------------ error state
+void set_error(const std::string& msg);
+int fail(int code, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+
+#define SPZ_CUDA(call)                                   \
+  do {                                                   \
+    cudaError_t e_ = (call);                             \
+    if (e_ != cudaSuccess) return ::spz::cuda_fail(e_, #call); \
+  } while (0)
+
+#define SPZ_CHECK_LAUNCH(what)                           \
+  do {                                                   \
+    cudaError_t e_ = cudaGetLastError();                 \
+    if (e_ != cudaSuccess) return ::spz::cuda_fail(e_, what); \
+  } while (0)
+
+// ------------------------------------------------------------ the handle
+struct Scratch {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+};
+
+}  // namespace spz
+
+struct spz_state_s {
+  uint32_t n = 0;
+  uint64_t N = 0;
+  double* re = nullptr;
+  double* im = nullptr;
+  bool owns = false;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  int device = 0;
+  // Reduction / planning scratch, grown on demand and reused.
+  spz::Scratch dev_scratch;
+  spz::Scratch host_scratch;  // pinned
+  // Two extra state vectors for adjoint differentiation (lazily allocated).
+  double* aux_re[2] = {nullptr, nullptr};
+  double* aux_im[2] = {nullptr, nullptr};
+};
+
+namespace spz {
+
+int ensure_dev_scratch(spz_state_t h, size_t bytes, void** out);
+int ensure_host_scratch(spz_state_t h, size_t bytes, void** out);
+int grid_for(uint64_t work, int threads = kThreads, int per_sm = 16);
+
+// ------------------------------------------------------ FP64 primitives
+// Adds and multiplies are issued as fused multiply-adds that round exactly
+// like the plain operation:  a*b == fma(a, b, -0.0),  a+b == fma(1, a, b),
+// a-b == fma(-1, b, a).  On GB300 the DFMA pipe issues ~18% faster than
+// DADD/DMUL, and the results are bit-identical.  Inline PTX keeps the
+// compiler from folding them back.  Negation flips the sign bit on the
+// integer pipe.
+__device__ __forceinline__ double dfma(double a, double b, double c) {
+  double d;
+  asm("fma.rn.f64 %0, %1, %2, %3;" : "=d"(d) : "d"(a), "d"(b), "d"(c));
+  return d;
+}
+__device__ __forceinline__ double dmul(double a, double b) { return dfma(a, b, -0.0); }
+__device__ __forceinline__ double dadd(double a, double b) { return dfma(1.0, a, b); }
+__device__ __forceinline__ double dsub(double a, double b) { return dfma(-1.0, b, a); }
+__device__ __forceinline__ double dneg(double a) {
+  return __longlong_as_double(__double_as_longlong(a) ^ (long long)0x8000000000000000ull);
+}
+
+// Insert a zero bit at each of the sorted positions pos[0] < pos[1] < ...
+// (so that the result has those bits clear and the other bits are k's bits in
+// order).  This enumerates the "s0" amplitudes of controlled gates.
+__device__ __forceinline__ uint64_t deposit(uint64_t k, const uint8_t* pos, int npos) {
+  for (int j = 0; j < npos; ++j) {
+    const uint64_t p = pos[j];
+    const uint64_t low = k & ((1ull << p) - 1);
+    k = ((k >> p) << (p + 1)) | low;
+  }
+  return k;
+}
+
+// ------------------------------------------------------ gate coefficients
+// Host-computed coefficients, exactly as the reference computes them
+// (glibc sin/cos, the same sub-expressions); see coef_for() in gates.cu.
+struct Coef {
+  double a, k, l, q, r, s, t;    // U: g = [(a,0), (k,l), (q,r), (s,t)]  (gates.rs:1285-1304)
+  double cs, sn, nsn;            // P: cos, sin; RX: cos, -, neg_sin; RY: cos, sin
+  double d0re, d0im, d1re, d1im; // RZ diagonal (gates.rs:930-937)
+};
+
+int coef_for(const spz_gate& g, Coef* out);
+
+// Validated, normalised description of one gate application.
+struct GateApp {
+  int kind;          // enum spz_gate_kind (H,X,Y,Z,P,RX,RY,RZ,U,SWAP)
+  uint32_t target;   // target (SWAP: q0)
+  uint32_t target2;  // SWAP: q1
+  uint64_t ones;     // controls that must read 1
+  uint64_t zeros;    // controls that must read 0
+  Coef c;
+};
+
+// Validate and build a GateApp (returns a status).
+int make_gate_app(uint32_t n, const spz_gate& g, uint32_t target, uint64_t ones, uint64_t zeros,
+                  GateApp* out);
+
+// True for gates whose matrix is diagonal (they need no amplitude pairing).
+inline bool is_diagonal(int kind) { return kind == SPZ_GATE_Z || kind == SPZ_GATE_P || kind == SPZ_GATE_RZ; }
+
+// Launch one gate over the whole state (the plain per-gate path).
+int launch_gate(spz_state_t h, const GateApp& g);
+
+// Algorithmic HBM bytes of one unfused gate application on 2^n amplitudes.
+uint64_t gate_algorithmic_bytes(uint32_t n, const GateApp& g);
+
+// FP64-pipe instructions (DFMA-issued adds, multiplies and FMAs) one gate
+// application needs on 2^n amplitudes.
+uint64_t gate_fp64_ops(uint32_t n, const GateApp& g);
+
+// Reductions used by measurement and the executor.
+int prob0_device(spz_state_t h, uint32_t target, double* out);
+int collapse_device(spz_state_t h, uint32_t target, int outcome, double scale);
+
+}  // namespace spz

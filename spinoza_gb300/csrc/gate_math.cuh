@@ -1,0 +1,85 @@
+// Per-pair and per-element gate arithmetic, shared by the plain per-gate
+// kernels and the fused tile executor.  Each function performs the reference's
+// floating-point operations in the reference's order (no contraction, FMA only
+// where the reference calls mul_add), so results are bit-identical to
+// spinoza's CPU path; the cited lines are in spinoza/src/gates.rs.
+//
+// (a, b) = (re, im) of s0 (target bit 0); (c, d) = (re, im) of s1.
+#pragma once
+
+#include "common.cuh"
+
+namespace spz {
+
+constexpr double kSqrtOneHalf = 0.70710678118654752440;  // math.rs:5
+
+template <int KIND>
+__device__ __forceinline__ void gate_pair(const Coef& g, double& a, double& b, double& c, double& d) {
+  if constexpr (KIND == SPZ_GATE_H) {  // h_apply_strat2, gates.rs:547-562
+    const double a1 = dmul(kSqrtOneHalf, a), b1 = dmul(kSqrtOneHalf, b);
+    const double c1 = dmul(kSqrtOneHalf, c), d1 = dmul(kSqrtOneHalf, d);
+    a = dadd(a1, c1);
+    b = dadd(b1, d1);
+    c = dsub(a1, c1);
+    d = dsub(b1, d1);
+  } else if constexpr (KIND == SPZ_GATE_X) {  // x_apply_target, gates.rs:329-334
+    double t = a; a = c; c = t;
+    t = b; b = d; d = t;
+  } else if constexpr (KIND == SPZ_GATE_Y) {  // y_proc_chunk, gates.rs:455-463
+    const double na = d, nb = dneg(c), nc = dneg(b), nd = a;
+    a = na; b = nb; c = nc; d = nd;
+  } else if constexpr (KIND == SPZ_GATE_Z) {  // z_proc_chunk, gates.rs:1054-1056
+    c = dneg(c);
+    d = dneg(d);
+  } else if constexpr (KIND == SPZ_GATE_P) {  // p_proc_chunk, gates.rs:837-838 (s1 only)
+    const double zr = c, zi = d;
+    c = dfma(zr, g.cs, dmul(zi, g.nsn));
+    d = dfma(zi, g.cs, dmul(zr, g.sn));
+  } else if constexpr (KIND == SPZ_GATE_RX) {  // rx_apply_target, gates.rs:713-725
+    const double na = dsub(dmul(a, g.cs), dmul(d, g.nsn));
+    const double nb = dadd(dmul(b, g.cs), dmul(c, g.nsn));
+    const double nc = dadd(dmul(b, g.sn), dmul(c, g.cs));  // b * -neg_sin + c * cos
+    const double nd = dadd(dmul(d, g.cs), dmul(a, g.nsn));
+    a = na; b = nb; c = nc; d = nd;
+  } else if constexpr (KIND == SPZ_GATE_RY) {  // ry_apply_strategy2, gates.rs:1116-1119
+    const double na = dsub(dmul(a, g.cs), dmul(c, g.sn));
+    const double nb = dsub(dmul(b, g.cs), dmul(d, g.sn));
+    const double nc = dadd(dmul(a, g.sn), dmul(c, g.cs));
+    const double nd = dadd(dmul(b, g.sn), dmul(d, g.cs));
+    a = na; b = nb; c = nc; d = nd;
+  } else if constexpr (KIND == SPZ_GATE_RZ) {  // rz_apply_strategy1, gates.rs:939-946
+    const double ar = a, ai = b, cr = c, ci = d;
+    a = dfma(ar, g.d0re, dmul(dneg(ai), g.d0im));
+    b = dfma(ar, g.d0im, dmul(ai, g.d0re));
+    c = dfma(cr, g.d1re, dmul(dneg(ci), g.d1im));
+    d = dfma(cr, g.d1im, dmul(ci, g.d1re));
+  } else if constexpr (KIND == SPZ_GATE_U) {  // u_apply_target, gates.rs:1256-1259
+    const double cc = a, dd = b, m = c, n = d;
+    const double t0 = dfma(g.a, cc, dfma(g.k, m, dmul(dneg(g.l), n)));
+    const double t1 = dfma(g.a, dd, dfma(g.k, n, dmul(g.l, m)));
+    const double t2 = dfma(g.q, cc, dfma(dneg(g.r), dd, dfma(g.s, m, dmul(dneg(g.t), n))));
+    const double t3 = dfma(g.q, dd, dfma(g.r, cc, dfma(g.s, n, dmul(g.t, m))));
+    a = t0; b = t1; c = t2; d = t3;
+  }
+}
+
+// Diagonal gates on one amplitude; `one` is the amplitude's target bit.
+template <int KIND>
+__device__ __forceinline__ void gate_diag(const Coef& g, bool one, double& re, double& im) {
+  if constexpr (KIND == SPZ_GATE_Z) {
+    if (one) { re = dneg(re); im = dneg(im); }
+  } else if constexpr (KIND == SPZ_GATE_P) {
+    if (one) {
+      const double zr = re, zi = im;
+      re = dfma(zr, g.cs, dmul(zi, g.nsn));
+      im = dfma(zi, g.cs, dmul(zr, g.sn));
+    }
+  } else if constexpr (KIND == SPZ_GATE_RZ) {
+    const double mre = one ? g.d1re : g.d0re, mim = one ? g.d1im : g.d0im;
+    const double cr = re, ci = im;
+    re = dfma(cr, mre, dmul(dneg(ci), mim));
+    im = dfma(cr, mim, dmul(ci, mre));
+  }
+}
+
+}  // namespace spz

@@ -1,0 +1,531 @@
+// Measurement, probability and expectation reductions, and sampling.
+// Replaces spinoza/src/measurement.rs:12-92 (measure_qubit) and the
+// reductions of spinoza/src/core.rs:65-264 (reservoir sampling,
+// qubit_expectation_value, xyz_expectation_value).
+//
+// All sums are deterministic: a fixed grid (a function of the size only),
+// each thread folding its strided elements in a fixed order, a fixed warp-
+// shuffle + shared-memory tree per block, then one block folding the block
+// partials in a fixed tree.  Results are identical from run to run.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "common.cuh"
+
+namespace spz {
+
+constexpr int kRedThreads = 256;
+constexpr int kMaxRedBlocks = kNumSMs * 8;  // 1216 partials per quantity
+
+__device__ __forceinline__ double block_sum(double v, double* smem) {
+  for (int off = 16; off > 0; off >>= 1) v = dadd(v, __shfl_down_sync(0xffffffffu, v, off));
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) smem[warp] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (warp == 0) {
+    r = lane < (int)(blockDim.x >> 5) ? smem[lane] : 0.0;
+    for (int off = 16; off > 0; off >>= 1) r = dadd(r, __shfl_down_sync(0xffffffffu, r, off));
+  }
+  __syncthreads();
+  return r;  // valid in thread 0
+}
+
+// Fold nq rows of `nblocks` partials each: out[q] = sum of partials[q][*].
+__global__ void finalize_kernel(const double* __restrict__ partials, int nblocks, int nq, double* __restrict__ out) {
+  __shared__ double smem[32];
+  for (int q = 0; q < nq; ++q) {
+    double v = 0.0;
+    for (int b = threadIdx.x; b < nblocks; b += blockDim.x) v = dadd(v, partials[(size_t)q * nblocks + b]);
+    v = block_sum(v, smem);
+    if (threadIdx.x == 0) out[q] = v;
+  }
+}
+
+enum RedMode { RED_PROB0 = 0, RED_X = 1, RED_Y = 2, RED_Z = 3, RED_NORM = 4 };
+
+// Per-pair functionals over the pairs (s0, s1 = s0 | tbit) with s0 enumerated
+// by inserting a zero at the target bit.  With tbit == 0 (RED_NORM) every
+// amplitude is one "pair" element s0.
+template <int MODE>
+__global__ void __launch_bounds__(kRedThreads) pair_reduce_kernel(const double* __restrict__ re,
+                                                                  const double* __restrict__ im, uint64_t nwork,
+                                                                  int t, double* __restrict__ partials) {
+  __shared__ double smem[32];
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t tbit = 1ull << t, lowmask = tbit - 1;
+  double acc = 0.0;
+  for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < nwork; w += stride) {
+    if constexpr (MODE == RED_NORM) {
+      const double a = re[w], b = im[w];
+      acc = dadd(acc, dfma(a, a, dmul(b, b)));
+    } else {
+      const uint64_t s0 = ((w & ~lowmask) << 1) | (w & lowmask);
+      const double a = re[s0], b = im[s0];
+      if constexpr (MODE == RED_PROB0) {
+        acc = dadd(acc, dfma(a, a, dmul(b, b)));
+      } else {
+        const uint64_t s1 = s0 | tbit;
+        const double c = re[s1], d = im[s1];
+        if constexpr (MODE == RED_X) {  // Re<psi|X psi> per pair: 2 (a c + b d)
+          acc = dadd(acc, dmul(2.0, dfma(a, c, dmul(b, d))));
+        } else if constexpr (MODE == RED_Y) {  // 2 (a d - b c)
+          acc = dadd(acc, dmul(2.0, dfma(a, d, dmul(dneg(b), c))));
+        } else {  // Z: |s0|^2 - |s1|^2
+          acc = dadd(acc, dsub(dfma(a, a, dmul(b, b)), dfma(c, c, dmul(d, d))));
+        }
+      }
+    }
+  }
+  const double s = block_sum(acc, smem);
+  if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
+// Launch a pair reduction, fold the partials into d_out[0] (device).
+template <int MODE>
+static int pair_reduce_to_device(spz_state_t h, int t, double* d_partials, double* d_out) {
+  const uint64_t nwork = MODE == RED_NORM ? h->N : h->N / 2;
+  const int blocks = std::min<int>(grid_for(nwork, kRedThreads, 8), kMaxRedBlocks);
+  pair_reduce_kernel<MODE><<<blocks, kRedThreads, 0, h->stream>>>(h->re, h->im, nwork, t, d_partials);
+  finalize_kernel<<<1, 1024, 0, h->stream>>>(d_partials, blocks, 1, d_out);
+  SPZ_CHECK_LAUNCH("pair_reduce_kernel");
+  return SPZ_OK;
+}
+
+// Read `count` doubles from the device into host memory (synchronises).
+static int read_back(spz_state_t h, const double* d_src, double* host, size_t count) {
+  void* pinned;
+  int rc = ensure_host_scratch(h, count * sizeof(double), &pinned);
+  if (rc) return rc;
+  SPZ_CUDA(cudaMemcpyAsync(pinned, d_src, count * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  SPZ_CUDA(cudaStreamSynchronize(h->stream));
+  std::copy((double*)pinned, (double*)pinned + count, host);
+  return SPZ_OK;
+}
+
+static int reduce_scalar(spz_state_t h, int mode, int t, double* out) {
+  void* scratch;
+  int rc = ensure_dev_scratch(h, (kMaxRedBlocks + 8) * sizeof(double), &scratch);
+  if (rc) return rc;
+  double* partials = (double*)scratch;
+  double* slot = partials + kMaxRedBlocks;
+  switch (mode) {
+    case RED_PROB0: rc = pair_reduce_to_device<RED_PROB0>(h, t, partials, slot); break;
+    case RED_X: rc = pair_reduce_to_device<RED_X>(h, t, partials, slot); break;
+    case RED_Y: rc = pair_reduce_to_device<RED_Y>(h, t, partials, slot); break;
+    case RED_Z: rc = pair_reduce_to_device<RED_Z>(h, t, partials, slot); break;
+    default: rc = pair_reduce_to_device<RED_NORM>(h, 0, partials, slot); break;
+  }
+  if (rc) return rc;
+  return read_back(h, slot, out, 1);
+}
+
+int norm_sqr_to_device(spz_state_t h, double* d_out) {
+  void* scratch;
+  int rc = ensure_dev_scratch(h, 64 * 1024 * sizeof(double), &scratch);
+  if (rc) return rc;
+  return pair_reduce_to_device<RED_NORM>(h, 0, (double*)scratch, d_out);
+}
+
+int prob0_device(spz_state_t h, uint32_t target, double* out) { return reduce_scalar(h, RED_PROB0, (int)target, out); }
+
+// ------------------------------------------------------------ collapse
+// measurement.rs:39-86: keep the measured half scaled by 1/sqrt(p), zero the other.
+__global__ void collapse_kernel(double* __restrict__ re, double* __restrict__ im, uint64_t nwork, int t,
+                                int outcome, double scale) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t tbit = 1ull << t, lowmask = tbit - 1;
+  for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < nwork; w += stride) {
+    const uint64_t s0 = ((w & ~lowmask) << 1) | (w & lowmask);
+    const uint64_t s1 = s0 | tbit;
+    const uint64_t keep = outcome ? s1 : s0, drop = outcome ? s0 : s1;
+    re[keep] = dmul(re[keep], scale);
+    im[keep] = dmul(im[keep], scale);
+    re[drop] = 0.0;
+    im[drop] = 0.0;
+  }
+}
+
+int collapse_device(spz_state_t h, uint32_t target, int outcome, double scale) {
+  collapse_kernel<<<grid_for(h->N / 2), kThreads, 0, h->stream>>>(h->re, h->im, h->N / 2, (int)target, outcome,
+                                                                   scale);
+  SPZ_CHECK_LAUNCH("collapse_kernel");
+  return SPZ_OK;
+}
+
+// measure_qubit (measurement.rs:12-92) with an explicit draw.
+int measure_qubit(spz_state_t h, uint32_t target, int reset, int forced, double u, uint8_t* outcome,
+                  double* prob0_out) {
+  if (target >= h->n) return fail(SPZ_ERR_INVALID_ARGUMENT, "target qubit out of range");
+  if (forced < -1 || forced > 1) return fail(SPZ_ERR_INVALID_ARGUMENT, "forced must be -1, 0 or 1");
+  double prob0;
+  int rc = prob0_device(h, target, &prob0);
+  if (rc) return rc;
+  const uint8_t val = forced >= 0 ? (uint8_t)forced : (uint8_t)(u < 1.0 - prob0 ? 1 : 0);
+  double scale;
+  if (val == 0) {
+    scale = 1.0 / std::sqrt(prob0);
+  } else {
+    const double prob1 = 1.0 - prob0;
+    scale = 1.0 / std::sqrt(prob1);
+  }
+  rc = collapse_device(h, target, val, scale);
+  if (rc) return rc;
+  if (val == 1 && reset) {  // measurement.rs:87-89
+    spz_gate x{};
+    x.kind = SPZ_GATE_X;
+    GateApp a;
+    rc = make_gate_app(h->n, x, target, 0, 0, &a);
+    if (!rc) rc = launch_gate(h, a);
+    if (rc) return rc;
+  }
+  if (outcome) *outcome = val;
+  if (prob0_out) *prob0_out = prob0;
+  return SPZ_OK;
+}
+
+// ------------------------------------------------------------ Pauli sums
+// Diagonal terms (x_mask == 0): sum_x |psi_x|^2 D(x), D(x) = sum_k c_k (-1)^popc(x & z_k).
+struct DiagTerms {
+  int nterms;
+  double coeff[64];
+  uint64_t zmask[64];
+};
+
+__global__ void __launch_bounds__(kRedThreads) diag_pauli_kernel(const double* __restrict__ re,
+                                                                 const double* __restrict__ im, uint64_t N,
+                                                                 DiagTerms T, double* __restrict__ partials) {
+  __shared__ double smem[32];
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  double acc = 0.0;
+  for (uint64_t x = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; x < N; x += stride) {
+    const double a = re[x], b = im[x];
+    const double p = dfma(a, a, dmul(b, b));
+    double dsum = 0.0;
+    for (int k = 0; k < T.nterms; ++k) {
+      const double ck = (__popcll(x & T.zmask[k]) & 1) ? dneg(T.coeff[k]) : T.coeff[k];
+      dsum = dadd(dsum, ck);
+    }
+    acc = dfma(p, dsum, acc);
+  }
+  const double s = block_sum(acc, smem);
+  if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
+// Terms sharing one x_mask != 0.  Pairs (x, y = x ^ xmask) with x's lowest
+// x_mask bit 0; w = conj(psi_x) psi_y.  For ny = popc(x_mask & z_mask):
+// even ny: term = i^ny (s_y + s_x) Re w; odd ny: term = -i^(ny-1) (s_y - s_x) Im w,
+// with s_x = (-1)^popc(x & z_mask).
+struct XTerms {
+  int nterms;
+  uint64_t xmask;
+  int lowbit;
+  double coeff[64];
+  uint64_t zmask[64];
+  int ny[64];
+};
+
+__global__ void __launch_bounds__(kRedThreads) x_pauli_kernel(const double* __restrict__ re,
+                                                              const double* __restrict__ im, uint64_t nwork,
+                                                              XTerms T, double* __restrict__ partials) {
+  __shared__ double smem[32];
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t lowmask = (1ull << T.lowbit) - 1;
+  double acc = 0.0;
+  for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < nwork; w += stride) {
+    const uint64_t x = ((w & ~lowmask) << 1) | (w & lowmask);
+    const uint64_t y = x ^ T.xmask;
+    const double a = re[x], b = im[x], c = re[y], d = im[y];
+    const double wre = dfma(a, c, dmul(b, d));
+    const double wim = dfma(a, d, dmul(dneg(b), c));
+    for (int k = 0; k < T.nterms; ++k) {
+      const int sx = (__popcll(x & T.zmask[k]) & 1) ? -1 : 1;
+      const int sy = (__popcll(y & T.zmask[k]) & 1) ? -1 : 1;
+      const int ny = T.ny[k] & 3;
+      double v;
+      if ((ny & 1) == 0) {
+        const int f = (sx + sy) * (ny == 0 ? 1 : -1);  // i^0 = 1, i^2 = -1
+        v = f == 0 ? 0.0 : (f > 0 ? (f == 2 ? dmul(2.0, wre) : wre) : (f == -2 ? dmul(-2.0, wre) : dneg(wre)));
+      } else {
+        const int f = (sy - sx) * (ny == 1 ? -1 : 1);  // Re(i (...)) = -Im, Re(-i (...)) = +Im
+        v = f == 0 ? 0.0 : (f > 0 ? dmul(2.0, wim) : dmul(-2.0, wim));
+      }
+      acc = dfma(T.coeff[k], v, acc);
+    }
+  }
+  const double s = block_sum(acc, smem);
+  if (threadIdx.x == 0) partials[blockIdx.x] = s;
+}
+
+int pauli_expectation(spz_state_t h, const spz_pauli_term* terms, size_t nterms, double* out) {
+  if (nterms && !terms) return fail(SPZ_ERR_NULL, "terms is NULL");
+  for (size_t k = 0; k < nterms; ++k)
+    if (h->n < 64 && ((terms[k].x_mask | terms[k].z_mask) >> h->n) != 0)
+      return fail(SPZ_ERR_INVALID_ARGUMENT, "Pauli term acts on a qubit out of range");
+  // Group: diagonal terms, then one group per distinct x_mask (chunks of 64 terms).
+  std::vector<std::vector<size_t>> groups;
+  std::vector<uint64_t> group_x;
+  for (size_t k = 0; k < nterms; ++k) {
+    size_t g = 0;
+    for (; g < groups.size(); ++g)
+      if (group_x[g] == terms[k].x_mask && groups[g].size() < 64) break;
+    if (g == groups.size()) {
+      groups.emplace_back();
+      group_x.push_back(terms[k].x_mask);
+    }
+    groups[g].push_back(k);
+  }
+  void* scratch;
+  const size_t ng = groups.size();
+  int rc = ensure_dev_scratch(h, ((ng + 1) * kMaxRedBlocks + ng + 8) * sizeof(double), &scratch);
+  if (rc) return rc;
+  double* partials = (double*)scratch;
+  double* slots = partials + (ng + 1) * kMaxRedBlocks;
+  for (size_t g = 0; g < ng; ++g) {
+    double* part = partials + g * kMaxRedBlocks;
+    if (group_x[g] == 0) {
+      DiagTerms T{};
+      T.nterms = (int)groups[g].size();
+      for (int j = 0; j < T.nterms; ++j) {
+        T.coeff[j] = terms[groups[g][j]].coeff;
+        T.zmask[j] = terms[groups[g][j]].z_mask;
+      }
+      const int blocks = std::min<int>(grid_for(h->N, kRedThreads, 8), kMaxRedBlocks);
+      diag_pauli_kernel<<<blocks, kRedThreads, 0, h->stream>>>(h->re, h->im, h->N, T, part);
+      finalize_kernel<<<1, 1024, 0, h->stream>>>(part, blocks, 1, slots + g);
+    } else {
+      XTerms T{};
+      T.nterms = (int)groups[g].size();
+      T.xmask = group_x[g];
+      T.lowbit = __builtin_ctzll(group_x[g]);
+      for (int j = 0; j < T.nterms; ++j) {
+        const spz_pauli_term& tm = terms[groups[g][j]];
+        T.coeff[j] = tm.coeff;
+        T.zmask[j] = tm.z_mask;
+        T.ny[j] = __builtin_popcountll(tm.x_mask & tm.z_mask);
+      }
+      const uint64_t nwork = h->N / 2;
+      const int blocks = std::min<int>(grid_for(nwork, kRedThreads, 8), kMaxRedBlocks);
+      x_pauli_kernel<<<blocks, kRedThreads, 0, h->stream>>>(h->re, h->im, nwork, T, part);
+      finalize_kernel<<<1, 1024, 0, h->stream>>>(part, blocks, 1, slots + g);
+    }
+    SPZ_CHECK_LAUNCH("pauli kernel");
+  }
+  std::vector<double> vals(ng);
+  if (ng) {
+    rc = read_back(h, slots, vals.data(), ng);
+    if (rc) return rc;
+  }
+  double total = 0.0;
+  for (size_t g = 0; g < ng; ++g) total += vals[g];
+  *out = total;
+  return SPZ_OK;
+}
+
+// ------------------------------------------------------------ sampling
+// Fixed blocked cumulative order (bit-identical to the oracle's restatement):
+// p_i = re*re + im*im; chunks of 256 amplitudes summed sequentially; super-
+// chunks of 1024 chunk totals summed sequentially; exclusive sequential scans
+// for the bases; per shot: target = u * total, first chunk whose end exceeds
+// the target, then a sequential running sum from the chunk's base.
+constexpr uint64_t kChunk = 256, kSuper = 1024;
+
+__device__ __forceinline__ double prob_exact(const double* re, const double* im, uint64_t i) {
+  const double r = re[i], m = im[i];
+  return dadd(dmul(r, r), dmul(m, m));
+}
+
+// One warp sums 32 chunks; chunk data is staged through shared memory so the
+// global loads are coalesced, then each lane folds its chunk in order.
+__global__ void __launch_bounds__(128) chunk_total_kernel(const double* __restrict__ re,
+                                                          const double* __restrict__ im, uint64_t nchunks,
+                                                          uint64_t cs, double* __restrict__ totals) {
+  __shared__ double tile[4][32][33];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const uint64_t warps_total = (uint64_t)gridDim.x * 4;
+  for (uint64_t c0 = ((uint64_t)blockIdx.x * 4 + warp) * 32; c0 < nchunks; c0 += warps_total * 32) {
+    double t = 0.0;
+    for (uint64_t j0 = 0; j0 < cs; j0 += 32) {
+      const uint64_t width = cs - j0 < 32 ? cs - j0 : 32;
+      for (int i = 0; i < 32; ++i) {
+        const uint64_t c = c0 + i;
+        if (c < nchunks && (uint64_t)lane < width) tile[warp][i][lane] = prob_exact(re, im, c * cs + j0 + lane);
+      }
+      __syncwarp();
+      if (c0 + lane < nchunks)
+        for (uint64_t j = 0; j < width; ++j) t = dadd(t, tile[warp][lane][j]);
+      __syncwarp();
+    }
+    if (c0 + lane < nchunks) totals[c0 + lane] = t;
+  }
+}
+
+// One thread per super-chunk: super total (sequential) .
+__global__ void super_total_kernel(const double* __restrict__ ct, uint64_t nchunks, uint64_t nsuper,
+                                   double* __restrict__ st) {
+  const uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (s >= nsuper) return;
+  double t = 0.0;
+  const uint64_t end = (s + 1) * kSuper < nchunks ? (s + 1) * kSuper : nchunks;
+  for (uint64_t c = s * kSuper; c < end; ++c) t = dadd(t, ct[c]);
+  st[s] = t;
+}
+
+// Single thread: super bases (exclusive sequential scan) and the total.
+__global__ void super_base_kernel(const double* __restrict__ st, uint64_t nsuper, double* __restrict__ sb,
+                                  double* __restrict__ total) {
+  double b = 0.0;
+  for (uint64_t s = 0; s < nsuper; ++s) {
+    sb[s] = b;
+    b = dadd(b, st[s]);
+  }
+  *total = b;
+}
+
+// One thread per super-chunk: chunk bases and chunk ends.
+__global__ void chunk_base_kernel(const double* __restrict__ ct, const double* __restrict__ sb,
+                                  const double* __restrict__ total, uint64_t nchunks, uint64_t nsuper,
+                                  double* __restrict__ cb, double* __restrict__ ce) {
+  const uint64_t s = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (s >= nsuper) return;
+  double pre = 0.0;
+  const uint64_t end = (s + 1) * kSuper < nchunks ? (s + 1) * kSuper : nchunks;
+  for (uint64_t c = s * kSuper; c < end; ++c) {
+    const double base = dadd(sb[s], pre);
+    cb[c] = base;
+    if (c > 0) ce[c - 1] = base;
+    pre = dadd(pre, ct[c]);
+  }
+  if (end == nchunks) ce[nchunks - 1] = *total;
+}
+
+__global__ void sample_kernel(const double* __restrict__ re, const double* __restrict__ im, uint64_t nchunks,
+                              uint64_t cs, const double* __restrict__ cb, const double* __restrict__ ce,
+                              const double* __restrict__ total_p, const double* __restrict__ u, uint64_t nshots,
+                              uint64_t* __restrict__ out) {
+  const uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (k >= nshots) return;
+  const double total = *total_p;
+  double target = dmul(u[k], total);
+  if (target >= total) target = nextafter(total, 0.0);
+  uint64_t lo = 0, hi = nchunks - 1;
+  while (lo < hi) {
+    const uint64_t mid = lo + (hi - lo) / 2;
+    if (ce[mid] > target) hi = mid; else lo = mid + 1;
+  }
+  const uint64_t c = lo;
+  double r = cb[c];
+  uint64_t outcome = ~0ull, last_pos = c * cs;
+  for (uint64_t j = 0; j < cs; ++j) {
+    const double pj = prob_exact(re, im, c * cs + j);
+    if (pj > 0.0) last_pos = c * cs + j;
+    r = dadd(r, pj);
+    if (r > target) {
+      outcome = c * cs + j;
+      break;
+    }
+  }
+  out[k] = outcome == ~0ull ? last_pos : outcome;
+}
+
+int sample(spz_state_t h, const double* u, size_t nshots, uint64_t* out) {
+  if (!u || !out) return fail(SPZ_ERR_NULL, "NULL argument");
+  if (nshots == 0) return SPZ_OK;
+  const uint64_t cs = std::min<uint64_t>(h->N, kChunk);
+  const uint64_t nchunks = h->N / cs;
+  const uint64_t nsuper = (nchunks + kSuper - 1) / kSuper;
+  // scratch: ct[nchunks] cb[nchunks] ce[nchunks] st[nsuper] sb[nsuper] total[1] u[nshots] out[nshots]
+  const size_t doubles = 3 * nchunks + 2 * nsuper + 8 + 2 * nshots;
+  void* scratch;
+  int rc = ensure_dev_scratch(h, doubles * sizeof(double), &scratch);
+  if (rc) return rc;
+  double* ct = (double*)scratch;
+  double* cb = ct + nchunks;
+  double* ce = cb + nchunks;
+  double* st = ce + nchunks;
+  double* sb = st + nsuper;
+  double* total = sb + nsuper;
+  double* du = total + 8;
+  uint64_t* dout = (uint64_t*)(du + nshots);
+  SPZ_CUDA(cudaMemcpyAsync(du, u, nshots * sizeof(double), cudaMemcpyDefault, h->stream));
+  const int cblocks = (int)std::min<uint64_t>((nchunks + 127) / 128, (uint64_t)kNumSMs * 16);
+  chunk_total_kernel<<<cblocks, 128, 0, h->stream>>>(h->re, h->im, nchunks, cs, ct);
+  super_total_kernel<<<(unsigned)((nsuper + 127) / 128), 128, 0, h->stream>>>(ct, nchunks, nsuper, st);
+  super_base_kernel<<<1, 1, 0, h->stream>>>(st, nsuper, sb, total);
+  chunk_base_kernel<<<(unsigned)((nsuper + 127) / 128), 128, 0, h->stream>>>(ct, sb, total, nchunks, nsuper, cb, ce);
+  sample_kernel<<<(unsigned)((nshots + 255) / 256), 256, 0, h->stream>>>(h->re, h->im, nchunks, cs, cb, ce, total,
+                                                                         du, nshots, dout);
+  SPZ_CHECK_LAUNCH("sampling kernels");
+  double host_total;
+  rc = read_back(h, total, &host_total, 1);
+  if (rc) return rc;
+  if (!(host_total > 0.0)) return fail(SPZ_ERR_INVALID_ARGUMENT, "state has zero norm");
+  SPZ_CUDA(cudaMemcpyAsync(out, dout, nshots * sizeof(uint64_t), cudaMemcpyDefault, h->stream));
+  SPZ_CUDA(cudaStreamSynchronize(h->stream));
+  return SPZ_OK;
+}
+
+}  // namespace spz
+
+using namespace spz;
+
+extern "C" {
+
+int spz_prob0(spz_state_t h, uint32_t target, double* prob0) {
+  if (!h || !prob0) return fail(SPZ_ERR_NULL, "NULL argument");
+  if (target >= h->n) return fail(SPZ_ERR_INVALID_ARGUMENT, "target qubit out of range");
+  return prob0_device(h, target, prob0);
+}
+
+int spz_measure_qubit(spz_state_t h, uint32_t target, int reset, int forced, double u, uint8_t* outcome,
+                      double* prob0) {
+  if (!h || !outcome) return fail(SPZ_ERR_NULL, "NULL argument");
+  return measure_qubit(h, target, reset, forced, u, outcome, prob0);
+}
+
+int spz_qubit_expectation_value(spz_state_t h, uint32_t target, double* out) {
+  if (!h || !out) return fail(SPZ_ERR_NULL, "NULL argument");
+  if (target >= h->n) return fail(SPZ_ERR_INVALID_ARGUMENT, "target qubit out of range");
+  double p0;
+  int rc = prob0_device(h, target, &p0);
+  if (rc) return rc;
+  *out = 2.0 * p0 - 1.0;  // core.rs:217
+  return SPZ_OK;
+}
+
+int spz_xyz_expectation_value(spz_state_t h, char observable, const uint32_t* targets, uint32_t ntargets,
+                              double* out) {
+  if (!h || (ntargets && (!targets || !out))) return fail(SPZ_ERR_NULL, "NULL argument");
+  int mode;
+  switch (observable) {
+    case 'x': mode = RED_X; break;
+    case 'y': mode = RED_Y; break;
+    case 'z': mode = RED_Z; break;
+    default: return fail(SPZ_ERR_INVALID_ARGUMENT, "observable must be 'x', 'y' or 'z' (core.rs:223-225)");
+  }
+  for (uint32_t i = 0; i < ntargets; ++i)
+    if (targets[i] >= h->n) return fail(SPZ_ERR_INVALID_ARGUMENT, "target qubit out of range");
+  for (uint32_t i = 0; i < ntargets; ++i) {
+    int rc = reduce_scalar(h, mode, (int)targets[i], &out[i]);
+    if (rc) return rc;
+  }
+  return SPZ_OK;
+}
+
+int spz_pauli_expectation(spz_state_t h, const spz_pauli_term* terms, size_t nterms, double* out) {
+  if (!h || !out) return fail(SPZ_ERR_NULL, "NULL argument");
+  return pauli_expectation(h, terms, nterms, out);
+}
+
+int spz_norm_sqr(spz_state_t h, double* out) {
+  if (!h || !out) return fail(SPZ_ERR_NULL, "NULL argument");
+  return reduce_scalar(h, RED_NORM, 0, out);
+}
+
+int spz_sample(spz_state_t h, const double* u, size_t nshots, uint64_t* out) {
+  if (!h) return fail(SPZ_ERR_NULL, "handle is NULL");
+  return sample(h, u, nshots, out);
+}
+
+}  // extern "C"

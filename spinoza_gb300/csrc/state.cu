@@ -1,0 +1,291 @@
+// State handles: allocation, wrapping of caller memory, host<->device copies,
+// reset, clone and seeded synthetic fills.  Replaces State::new / Clone and the
+// public reals/imags fields of spinoza/src/core.rs:18-51.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <string>
+
+#include "common.cuh"
+
+namespace spz {
+
+namespace {
+thread_local std::string g_last_error;
+}
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+int fail(int code, const std::string& msg) {
+  set_error(msg);
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  set_error(std::string("CUDA error in ") + what + ": " + cudaGetErrorString(e));
+  return e == cudaErrorMemoryAllocation ? SPZ_ERR_OUT_OF_MEMORY : SPZ_ERR_CUDA;
+}
+
+int grid_for(uint64_t work, int threads, int per_sm) {
+  uint64_t blocks = (work + threads - 1) / threads;
+  uint64_t cap = (uint64_t)kNumSMs * per_sm;
+  if (blocks > cap) blocks = cap;
+  if (blocks < 1) blocks = 1;
+  return (int)blocks;
+}
+
+int ensure_dev_scratch(spz_state_t h, size_t bytes, void** out) {
+  if (h->dev_scratch.bytes < bytes) {
+    if (h->dev_scratch.ptr) {
+      SPZ_CUDA(cudaStreamSynchronize(h->stream));
+      SPZ_CUDA(cudaFree(h->dev_scratch.ptr));
+      h->dev_scratch.ptr = nullptr;
+      h->dev_scratch.bytes = 0;
+    }
+    size_t sz = bytes < 4096 ? 4096 : bytes;
+    SPZ_CUDA(cudaMalloc(&h->dev_scratch.ptr, sz));
+    h->dev_scratch.bytes = sz;
+  }
+  *out = h->dev_scratch.ptr;
+  return SPZ_OK;
+}
+
+int ensure_host_scratch(spz_state_t h, size_t bytes, void** out) {
+  if (h->host_scratch.bytes < bytes) {
+    if (h->host_scratch.ptr) {
+      SPZ_CUDA(cudaStreamSynchronize(h->stream));
+      SPZ_CUDA(cudaFreeHost(h->host_scratch.ptr));
+      h->host_scratch.ptr = nullptr;
+      h->host_scratch.bytes = 0;
+    }
+    size_t sz = bytes < 4096 ? 4096 : bytes;
+    SPZ_CUDA(cudaMallocHost(&h->host_scratch.ptr, sz));
+    h->host_scratch.bytes = sz;
+  }
+  *out = h->host_scratch.ptr;
+  return SPZ_OK;
+}
+
+// ------------------------------------------------------------ kernels
+__global__ void zero_state_kernel(double* __restrict__ re, double* __restrict__ im, uint64_t N) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < N; i += stride) {
+    re[i] = i == 0 ? 1.0 : 0.0;
+    im[i] = 0.0;
+  }
+}
+
+// Counter-based splitmix64 stream: u64(seed, i) = mix(mix(seed + G) + (i+1) G).
+__host__ __device__ __forceinline__ uint64_t mix64(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+constexpr uint64_t kGolden = 0x9E3779B97F4A7C15ull;
+
+__device__ __forceinline__ double stream_uniform(uint64_t key, uint64_t i) {
+  return (double)(mix64(key + (i + 1) * kGolden) >> 11) * 0x1.0p-53;
+}
+
+// dist 0: uniform [-1,1) (exact, bit-reproducible on the host);
+// dist 1: N(0,1) via Box-Muller on the pair (u(2i), u(2i+1)).
+__global__ void fill_kernel(double* __restrict__ re, double* __restrict__ im, uint64_t N, uint64_t key,
+                            int dist) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < N; i += stride) {
+    double u1 = stream_uniform(key, 2 * i), u2 = stream_uniform(key, 2 * i + 1);
+    if (dist == 0) {
+      re[i] = dadd(dmul(2.0, u1), -1.0);
+      im[i] = dadd(dmul(2.0, u2), -1.0);
+    } else {
+      double r = sqrt(-2.0 * log(1.0 - u1));
+      double s, c;
+      sincospi(2.0 * u2, &s, &c);
+      re[i] = r * c;
+      im[i] = r * s;
+    }
+  }
+}
+
+__global__ void scale_kernel(double* __restrict__ re, double* __restrict__ im, uint64_t N,
+                             const double* __restrict__ scale_ptr) {
+  const double s = *scale_ptr;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < N; i += stride) {
+    re[i] = dmul(re[i], s);
+    im[i] = dmul(im[i], s);
+  }
+}
+
+__global__ void rsqrt_kernel(double* p) { p[1] = 1.0 / sqrt(p[0]); }
+
+int norm_sqr_to_device(spz_state_t h, double* d_out);  // reduce.cu
+
+}  // namespace spz
+
+using namespace spz;
+
+// ================================================================== C ABI
+extern "C" {
+
+const char* spz_last_error(void) { return g_last_error.c_str(); }
+
+const char* spz_version(void) { return "spinoza_gb300 0.1.0 sm_103a"; }
+
+static int alloc_handle(uint32_t n, spz_state_t* out) {
+  if (!out) return fail(SPZ_ERR_NULL, "out is NULL");
+  if (n == 0) return fail(SPZ_ERR_INVALID_ARGUMENT, "n must be > 0 (core.rs:33 asserts n > 0)");
+  if (n > kMaxQubits) return fail(SPZ_ERR_INVALID_ARGUMENT, "n exceeds SPZ_MAX_QUBITS");
+  spz_state_t h = new (std::nothrow) spz_state_s();
+  if (!h) return fail(SPZ_ERR_OUT_OF_MEMORY, "host allocation of handle failed");
+  h->n = n;
+  h->N = 1ull << n;
+  cudaError_t e = cudaGetDevice(&h->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete h;
+    return cuda_fail(e, "stream creation");
+  }
+  h->stream = h->own_stream;
+  *out = h;
+  return SPZ_OK;
+}
+
+int spz_state_create(uint32_t n, spz_state_t* out) {
+  int rc = alloc_handle(n, out);
+  if (rc) return rc;
+  spz_state_t h = *out;
+  cudaError_t e = cudaMalloc(&h->re, h->N * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&h->im, h->N * sizeof(double));
+  if (e != cudaSuccess) {
+    if (h->re) cudaFree(h->re);
+    cudaStreamDestroy(h->own_stream);
+    delete h;
+    *out = nullptr;
+    return cuda_fail(e, "cudaMalloc of the state");
+  }
+  h->owns = true;
+  rc = spz_state_reset_zero(h);
+  if (rc) {
+    spz_state_destroy(h);
+    *out = nullptr;
+  }
+  return rc;
+}
+
+int spz_state_wrap(uint32_t n, double* d_reals, double* d_imags, spz_state_t* out) {
+  if (!d_reals || !d_imags) return fail(SPZ_ERR_NULL, "device arrays are NULL");
+  if (((uintptr_t)d_reals & 15) || ((uintptr_t)d_imags & 15))
+    return fail(SPZ_ERR_INVALID_ARGUMENT, "device arrays must be 16-byte aligned");
+  int rc = alloc_handle(n, out);
+  if (rc) return rc;
+  (*out)->re = d_reals;
+  (*out)->im = d_imags;
+  (*out)->owns = false;
+  return SPZ_OK;
+}
+
+int spz_state_destroy(spz_state_t h) {
+  if (!h) return SPZ_OK;
+  cudaStreamSynchronize(h->stream);
+  if (h->owns) {
+    cudaFree(h->re);
+    cudaFree(h->im);
+  }
+  for (int j = 0; j < 2; ++j) {
+    if (h->aux_re[j]) cudaFree(h->aux_re[j]);
+    if (h->aux_im[j]) cudaFree(h->aux_im[j]);
+  }
+  if (h->dev_scratch.ptr) cudaFree(h->dev_scratch.ptr);
+  if (h->host_scratch.ptr) cudaFreeHost(h->host_scratch.ptr);
+  if (h->own_stream) cudaStreamDestroy(h->own_stream);
+  delete h;
+  return SPZ_OK;
+}
+
+int spz_state_set_stream(spz_state_t h, void* stream) {
+  if (!h) return fail(SPZ_ERR_NULL, "handle is NULL");
+  h->stream = stream ? (cudaStream_t)stream : h->own_stream;
+  return SPZ_OK;
+}
+
+int spz_state_synchronize(spz_state_t h) {
+  if (!h) return fail(SPZ_ERR_NULL, "handle is NULL");
+  SPZ_CUDA(cudaStreamSynchronize(h->stream));
+  return SPZ_OK;
+}
+
+int spz_state_num_qubits(spz_state_t h, uint32_t* n) {
+  if (!h || !n) return fail(SPZ_ERR_NULL, "NULL argument");
+  *n = h->n;
+  return SPZ_OK;
+}
+
+int spz_state_device_arrays(spz_state_t h, double** d_reals, double** d_imags) {
+  if (!h || !d_reals || !d_imags) return fail(SPZ_ERR_NULL, "NULL argument");
+  *d_reals = h->re;
+  *d_imags = h->im;
+  return SPZ_OK;
+}
+
+int spz_state_upload(spz_state_t h, const double* reals, const double* imags) {
+  if (!h || !reals || !imags) return fail(SPZ_ERR_NULL, "NULL argument");
+  SPZ_CUDA(cudaMemcpyAsync(h->re, reals, h->N * sizeof(double), cudaMemcpyDefault, h->stream));
+  SPZ_CUDA(cudaMemcpyAsync(h->im, imags, h->N * sizeof(double), cudaMemcpyDefault, h->stream));
+  SPZ_CUDA(cudaStreamSynchronize(h->stream));
+  return SPZ_OK;
+}
+
+int spz_state_download(spz_state_t h, double* reals, double* imags) {
+  if (!h || !reals || !imags) return fail(SPZ_ERR_NULL, "NULL argument");
+  SPZ_CUDA(cudaMemcpyAsync(reals, h->re, h->N * sizeof(double), cudaMemcpyDefault, h->stream));
+  SPZ_CUDA(cudaMemcpyAsync(imags, h->im, h->N * sizeof(double), cudaMemcpyDefault, h->stream));
+  SPZ_CUDA(cudaStreamSynchronize(h->stream));
+  return SPZ_OK;
+}
+
+int spz_state_reset_zero(spz_state_t h) {
+  if (!h) return fail(SPZ_ERR_NULL, "handle is NULL");
+  zero_state_kernel<<<grid_for(h->N), kThreads, 0, h->stream>>>(h->re, h->im, h->N);
+  SPZ_CHECK_LAUNCH("zero_state_kernel");
+  return SPZ_OK;
+}
+
+int spz_state_copy(spz_state_t dst, spz_state_t src) {
+  if (!dst || !src) return fail(SPZ_ERR_NULL, "handle is NULL");
+  if (dst->n != src->n) return fail(SPZ_ERR_INVALID_ARGUMENT, "qubit counts differ");
+  if (dst == src) return SPZ_OK;
+  // Order after src's pending work, then run on dst's stream.
+  cudaEvent_t ev;
+  SPZ_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  SPZ_CUDA(cudaEventRecord(ev, src->stream));
+  SPZ_CUDA(cudaStreamWaitEvent(dst->stream, ev, 0));
+  SPZ_CUDA(cudaEventDestroy(ev));
+  SPZ_CUDA(cudaMemcpyAsync(dst->re, src->re, dst->N * sizeof(double), cudaMemcpyDeviceToDevice, dst->stream));
+  SPZ_CUDA(cudaMemcpyAsync(dst->im, src->im, dst->N * sizeof(double), cudaMemcpyDeviceToDevice, dst->stream));
+  return SPZ_OK;
+}
+
+int spz_state_fill_random(spz_state_t h, uint64_t seed, int dist, int normalise) {
+  if (!h) return fail(SPZ_ERR_NULL, "handle is NULL");
+  if (dist != 0 && dist != 1) return fail(SPZ_ERR_INVALID_ARGUMENT, "dist must be 0 or 1");
+  const uint64_t key = mix64(seed + kGolden);
+  fill_kernel<<<grid_for(h->N), kThreads, 0, h->stream>>>(h->re, h->im, h->N, key, dist);
+  SPZ_CHECK_LAUNCH("fill_kernel");
+  if (normalise) {
+    void* scratch;
+    int rc = ensure_dev_scratch(h, 64 * 1024 * sizeof(double), &scratch);
+    if (rc) return rc;
+    // norm_sqr_to_device writes the sum to the last two slots of scratch
+    double* slot = (double*)scratch + 64 * 1024 - 2;
+    rc = norm_sqr_to_device(h, slot);
+    if (rc) return rc;
+    rsqrt_kernel<<<1, 1, 0, h->stream>>>(slot);
+    scale_kernel<<<grid_for(h->N), kThreads, 0, h->stream>>>(h->re, h->im, h->N, slot + 1);
+    SPZ_CHECK_LAUNCH("scale_kernel");
+  }
+  return SPZ_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,240 @@
+"""The fused circuit executor vs the oracle's sequential execute().
+
+The planner only reorders gates where the swap is bit-exact, and each gate's
+arithmetic inside a tile is the plain kernel's, so fused results are expected
+to be bit-identical; the asserted bound is the benchmark spec's 1e-12 plus an exact
+check where the circuit allows it."""
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+from spinoza_gb300 import _native as nat
+from spinoza_gb300 import circuit, rng
+from spinoza_gb300.circuit import QuantumCircuit, QuantumRegister
+from spinoza_gb300.core import State
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-12
+
+
+def _run_gpu(n, ops, init, fused=True, tracker=(0, 0)):
+    s = State.from_arrays(*init)
+    qc = QuantumCircuit.from_state(s, fused=fused)
+    qc.qubit_tracker.c.measured, qc.qubit_tracker.c.values = tracker
+    qc.execute_ops(ops)
+    return s.to_numpy(), (qc.qubit_tracker.c.measured, qc.qubit_tracker.c.values), qc.last_stats
+
+
+def _run_oracle(ops, init, tracker=(0, 0)):
+    re, im = init[0].copy(), init[1].copy()
+    tr = oracle.execute(ops, re, im, *tracker)
+    return (re, im), tr
+
+
+def _builder():
+    qc = QuantumCircuit.__new__(QuantumCircuit)
+    qc.transformations = []
+    qc._seed, qc._draw_index = 0, 0
+    return qc
+
+
+def qft_with_swaps(n):
+    """Config 1: for j = n-1..0: H(j), CP(pi/2^(j-k)) k < j; then SWAP(i, n-1-i)."""
+    qc = _builder()
+    for j in range(n - 1, -1, -1):
+        qc.h(j)
+        for k in range(j - 1, -1, -1):
+            qc.cp(math.pi / 2 ** (j - k), j, k)
+    for i in range(n // 2):
+        qc.swap(i, n - 1 - i)
+    return qc.ops()
+
+
+def brickwork(n, layers, seed=2):
+    """Config 2 shape: U(theta, phi, lambda) on every qubit, then CX even, CX odd."""
+    qc = _builder()
+    ang = rng.uniforms(seed, 3 * n * layers) * 2 * math.pi
+    k = 0
+    for _ in range(layers):
+        for q in range(n):
+            qc.u(ang[k], ang[k + 1], ang[k + 2], q)
+            k += 3
+        for q in range(0, n - 1, 2):
+            qc.cx(q, q + 1)
+        for q in range(1, n - 1, 2):
+            qc.cx(q, q + 1)
+    return qc.ops()
+
+
+def random_circuit(n, ngates, seed):
+    """Every gate kind, with none / single / ones / mixed controls."""
+    r = np.random.default_rng(seed)
+    ops = np.zeros(ngates, dtype=nat.OP_DTYPE)
+    kinds = [nat.H, nat.X, nat.Y, nat.Z, nat.P, nat.RX, nat.RY, nat.RZ, nat.U, nat.SWAP]
+    for i in range(ngates):
+        k = int(r.choice(kinds))
+        q = r.permutation(n)
+        t, t2 = int(q[0]), int(q[1])
+        nc = int(r.integers(0, 4))
+        ctrls = [int(c) for c in q[2:2 + nc]]
+        ck = [nat.CONTROLS_NONE, nat.CONTROLS_SINGLE, nat.CONTROLS_ONES, nat.CONTROLS_ONES][nc]
+        zeros = 0
+        if nc >= 2 and r.random() < 0.5:
+            ck = nat.CONTROLS_MIXED
+            zeros = 1 << ctrls[0]
+        cm = sum(1 << c for c in ctrls)
+        p = r.uniform(-math.pi, math.pi, 3)
+        ops[i] = ((k, t, t2, 0, p), t, ck, cm, zeros)
+    return ops
+
+
+def _compare(a, b, exact=True):
+    (gre, gim), (ore, oim) = a, b
+    d = max(np.max(np.abs(gre - ore)), np.max(np.abs(gim - oim)))
+    assert d <= TOL, d
+    if exact:
+        assert np.array_equal(gre, ore) and np.array_equal(gim, oim), d
+
+
+def test_qft20_config1_parity(gpu):
+    """Config 1: QFT with swaps on a seeded N(0,1) normalised 20-qubit state."""
+    n = 20
+    init = rng.normal_state(n, 1)
+    ops = qft_with_swaps(n)
+    g, _, st = _run_gpu(n, ops, init)
+    o, _ = _run_oracle(ops, init)
+    _compare(g, o)
+    assert st.passes < 20 and st.gates == 220
+    gu, _, stu = _run_gpu(n, ops, init, fused=False)
+    _compare(gu, o)
+    assert stu.passes == 220
+
+
+@pytest.mark.parametrize("n,layers", [(12, 3), (17, 2)])
+def test_brickwork_parity(gpu, n, layers):
+    init = rng.uniform_state(n, 5)
+    ops = brickwork(n, layers)
+    g, _, st = _run_gpu(n, ops, init)
+    o, _ = _run_oracle(ops, init)
+    _compare(g, o)
+    assert st.tile_passes >= 1
+
+
+@pytest.mark.parametrize("n,seed", [(6, 1), (13, 2), (15, 3)])
+def test_random_circuits_fused_equals_oracle(gpu, n, seed):
+    init = rng.uniform_state(n, seed)
+    ops = random_circuit(n, 300, seed)
+    g, _, _ = _run_gpu(n, ops, init)
+    o, _ = _run_oracle(ops, init)
+    _compare(g, o)
+    gu, _, _ = _run_gpu(n, ops, init, fused=False)
+    _compare(gu, o)
+
+
+def test_mid_circuit_measurement_and_classical_control(gpu):
+    """circuit.rs:559-578: M records the outcome; a Single control on a measured
+    qubit becomes a classical condition."""
+    n = 8
+    init = rng.normal_state(n, 3)
+    qc = _builder()
+    for q in range(n):
+        qc.h(q)
+    qc.measure(2)
+    qc.cx(2, 5)      # classical: applies iff qubit 2 measured 1
+    qc.crx(0.3, 2, 6)
+    qc.ry(0.4, 2)
+    qc.measure(7)
+    qc.cx(7, 0)
+    qc.measure(2)    # already measured: no-op
+    ops = qc.ops()
+    for u in (0.1, 0.9):
+        ops["gate"]["p"][[n, n + 4], 0] = u  # the two fresh measurement draws
+        g, gtr, _ = _run_gpu(n, ops, init)
+        o, otr = _run_oracle(ops, init)
+        assert gtr == otr
+        _compare(g, o)
+
+
+def test_reference_circuit_tests(gpu):
+    """circuit.rs:725-822, 962-989, 1030-1061, 1234-1250 restated on the device."""
+    # append: H on two one-qubit registers -> 0.5 everywhere
+    qr0, qr1 = QuantumRegister(1), QuantumRegister(1)
+    qc = QuantumCircuit(qr0, qr1)
+    one = QuantumCircuit(QuantumRegister(1))
+    one.h(0)
+    qc.append(one, qr0)
+    qc.append(one, qr1)
+    qc.execute()
+    re, im = qc.state.to_numpy()
+    np.testing.assert_allclose(re, 0.5, atol=1e-4)
+    np.testing.assert_allclose(im, 0.0, atol=1e-4)
+    # inverse: [H(0), P(pi/4, 1)].inverse() == [P(-pi/4, 1), H(0)]
+    a = QuantumCircuit(QuantumRegister(2))
+    a.h(0)
+    a.p(math.pi / 4, 1)
+    a.inverse()
+    a.execute()
+    b = QuantumCircuit(QuantumRegister(2))
+    b.p(-math.pi / 4, 1)
+    b.h(0)
+    b.execute()
+    assert all(np.array_equal(x, y) for x, y in zip(a.state.to_numpy(), b.state.to_numpy()))
+    # all_gates_as_transformations (N = 17): circuit == functional API
+    from spinoza_gb300 import gates as G
+    from spinoza_gb300.gates import Gate
+
+    N, PI = 17, math.pi
+    q = QuantumCircuit(QuantumRegister(N))
+    for t in range(N):
+        q.h(t)
+    q.x(0); q.y(1); q.z(2); q.p(PI, 3); q.cp(PI, 3, 4); q.rx(PI, 5); q.ry(PI, 6); q.rz(PI, 7)
+    q.u(PI, PI, PI, 8); q.cy(9, 10); q.crx(PI, 11, 12); q.cry(PI, 13, 14)
+    q.execute()
+    s = State(N)
+    for t in range(N):
+        G.apply(Gate.H, s, t)
+    G.apply(Gate.X, s, 0); G.apply(Gate.Y, s, 1); G.apply(Gate.Z, s, 2); G.apply(Gate.P(PI), s, 3)
+    G.c_apply(Gate.P(PI), s, 3, 4); G.apply(Gate.RX(PI), s, 5); G.apply(Gate.RY(PI), s, 6)
+    G.apply(Gate.RZ(PI), s, 7); G.apply(Gate.U(PI, PI, PI), s, 8); G.c_apply(Gate.Y, s, 9, 10)
+    G.c_apply(Gate.RX(PI), s, 11, 12); G.c_apply(Gate.RY(PI), s, 13, 14)
+    assert all(np.array_equal(x, y) for x, y in zip(q.state.to_numpy(), s.to_numpy()))
+
+
+def test_swap_all_qubits_circuit_equals_three_cx(gpu):
+    """circuit.rs:891-929."""
+    n = 9
+    init = rng.uniform_state(n, 4)
+    qc = _builder()
+    for i in range(n >> 1):
+        qc.swap(i, n - 1 - i)
+    a, _, _ = _run_gpu(n, qc.ops(), init)
+    qc = _builder()
+    for i in range(n >> 1):
+        j = n - 1 - i
+        qc.cx(i, j); qc.cx(j, i); qc.cx(i, j)
+    b, _, _ = _run_gpu(n, qc.ops(), init)
+    _compare(a, b)
+
+
+def test_iqft_device_entry_point(gpu):
+    from spinoza_gb300.core import iqft
+
+    n = 11
+    init = rng.normal_state(n, 6)
+    s = State.from_arrays(*init)
+    t = list(range(n - 1, -1, -1))
+    iqft(s, t)
+    re, im = init[0].copy(), init[1].copy()
+    oracle.iqft(re, im, t)
+    _compare(s.to_numpy(), (re, im))
+
+
+def test_plan_stats_agree_with_execution(gpu):
+    n = 14
+    ops = brickwork(n, 3)
+    planned = circuit.plan_stats(n, ops)
+    _, _, st = _run_gpu(n, ops, rng.uniform_state(n, 1))
+    assert planned["passes"] == st.passes and planned["bytes_moved"] == st.bytes_moved

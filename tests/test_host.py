@@ -1,0 +1,155 @@
+"""Host-side checks that need no GPU: the C-ABI library loads and exports every
+declared entry point, struct layouts match, the RNG streams agree bit for bit
+with the oracle, and the fusion planner's decisions."""
+import math
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import oracle
+from spinoza_gb300 import _native as nat
+from spinoza_gb300 import circuit, rng
+from spinoza_gb300.circuit import QuantumCircuit, QuantumRegister
+from spinoza_gb300.gates import Gate
+
+HEADER = Path(__file__).resolve().parent.parent / "include" / "spinoza_gb300.h"
+
+
+def declared_functions():
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\**\s+\**(spz_\w+)\s*\(", text, flags=re.M)))
+
+
+def test_library_exports_every_declared_symbol(native):
+    names = declared_functions()
+    assert len(names) >= 30
+    for name in names:
+        assert hasattr(native, name), name
+    assert {s[0] for s in nat.SIGNATURES} == set(names)
+
+
+def test_version(native):
+    assert native.spz_version().decode().startswith("spinoza_gb300")
+
+
+def test_struct_layouts():
+    import ctypes
+
+    assert ctypes.sizeof(nat.spz_gate) == 40
+    assert ctypes.sizeof(nat.spz_op) == 64
+    assert ctypes.sizeof(nat.spz_pauli_term) == 24
+    assert ctypes.sizeof(nat.spz_exec_stats) == 64
+
+
+def test_rng_stream_matches_oracle():
+    u = rng.uniforms(1234, 64, start=10)
+    for i in range(64):
+        assert u[i] == oracle.stream_uniform(1234, 10 + i)
+
+
+def test_uniform_state_matches_oracle():
+    re, im = rng.uniform_state(10, 77)
+    ore, oim = oracle.uniform_state(10, 77)
+    assert np.array_equal(re, ore) and np.array_equal(im, oim)
+
+
+def test_normal_state_is_normalised():
+    re, im = rng.normal_state(12, 1)
+    assert abs(np.sum(re * re + im * im) - 1.0) < 1e-12
+
+
+# ------------------------------------------------------------------- planner
+def qft_ops(n):
+    qc = QuantumCircuit.__new__(QuantumCircuit)
+    qc.transformations = []
+    for j in range(n - 1, -1, -1):
+        qc.h(j)
+        for k in range(j - 1, -1, -1):
+            qc.cp(math.pi / 2 ** (j - k), j, k)
+    for i in range(n // 2):
+        qc.swap(i, n - 1 - i)
+    return circuit._ops_array(qc.transformations, lambda: 0.0)
+
+
+def brickwork_ops(n, layers, seed=2):
+    qc = QuantumCircuit.__new__(QuantumCircuit)
+    qc.transformations = []
+    ang = rng.uniforms(seed, 3 * n * layers) * 2 * math.pi
+    k = 0
+    for _ in range(layers):
+        for q in range(n):
+            qc.u(ang[k], ang[k + 1], ang[k + 2], q)
+            k += 3
+        for q in range(0, n - 1, 2):
+            qc.cx(q, q + 1)
+        for q in range(1, n - 1, 2):
+            qc.cx(q, q + 1)
+    return circuit._ops_array(qc.transformations, lambda: 0.0)
+
+
+def test_planner_fuses_qft(native):
+    ops = qft_ops(20)
+    st = circuit.plan_stats(20, ops)
+    unf = circuit.plan_stats(20, ops, fused=False)
+    assert st["gates"] == unf["gates"] == 20 + 190 + 10
+    assert unf["passes"] == 220
+    assert st["passes"] <= 12, st
+    assert st["bytes_moved"] < unf["bytes_moved"]
+
+
+def test_planner_fuses_brickwork(native):
+    n, layers = 30, 2
+    ops = brickwork_ops(n, layers)
+    st = circuit.plan_stats(n, ops)
+    assert st["gates"] == layers * (n + n - 1)
+    assert st["passes"] < st["gates"] / 4, st
+    # the algorithmic bytes are the unfused minimum
+    assert st["algorithmic_bytes"] == layers * (n * 32 + (n - 1) * 16) << n
+
+
+def test_planner_measurement_is_a_barrier(native):
+    ops = np.zeros(3, dtype=nat.OP_DTYPE)
+    ops[0] = ((nat.H, 0, 0, 0, (0, 0, 0)), 0, 0, 0, 0)
+    ops[1] = ((nat.M, 0, 0, 0, (0.5, 0, 0)), 1, 0, 0, 0)
+    ops[2] = ((nat.H, 0, 0, 0, (0, 0, 0)), 0, 0, 0, 0)
+    st = circuit.plan_stats(4, ops)
+    assert st["gates"] == 2 and st["passes"] == 1 + 2 + 1
+
+
+def test_invalid_ops_are_rejected_on_the_host(native):
+    ops = np.zeros(1, dtype=nat.OP_DTYPE)
+    ops[0] = ((nat.H, 0, 0, 0, (0, 0, 0)), 7, 0, 0, 0)  # target 7 on 4 qubits
+    with pytest.raises(ValueError):
+        circuit.plan_stats(4, ops)
+    ops[0] = ((nat.X, 0, 0, 0, (0, 0, 0)), 1, nat.CONTROLS_SINGLE, 1 << 1, 0)  # control == target
+    with pytest.raises(ValueError):
+        circuit.plan_stats(4, ops)
+    ops[0] = ((nat.UNITARY, 0, 0, 0, (0, 0, 0)), 0, 0, 0, 0)
+    with pytest.raises(NotImplementedError):
+        circuit.plan_stats(4, ops)
+
+
+def test_circuit_builders_mirror_reference(native):
+    """circuit.rs: register shifts, Controls::from, new_with_control, inverse."""
+    a, b = QuantumRegister(2), QuantumRegister(3)
+    qc = QuantumCircuit.__new__(QuantumCircuit)
+    qc.transformations = []
+    QuantumCircuit.__init__  # registers are shifted by the constructor:
+    bits = 0
+    for r in (a, b):
+        r.update_shift(bits)
+        bits += len(r)
+    assert a.qubits == [0, 1] and b.qubits == [2, 3, 4] and b.get_shift() == 2
+    from spinoza_gb300.circuit import Controls
+
+    c = Controls.single(0).new_with_control(3, 1)
+    assert c.kind == Controls.ONES and c.controls == [1, 3]
+    m = Controls.mixed([0], {0}).new_with_control(2, 1)
+    assert m.kind == Controls.MIXED and m.controls == [1, 2] and m.zeros == {1}
+    qc.h(0)
+    qc.p(math.pi / 4, 1)
+    qc.inverse()
+    assert qc.transformations[0].gate == Gate.P(-math.pi / 4) and qc.transformations[1].gate == Gate.H
