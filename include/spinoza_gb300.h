@@ -200,6 +200,13 @@ int spz_circuit_execute(spz_state_t h, const spz_op* ops, size_t nops, spz_track
  * measurement outcome as 0.  For inspecting how a circuit is fused. */
 int spz_plan_stats(uint32_t n, const spz_op* ops, size_t nops, uint32_t flags, spz_exec_stats* stats);
 
+/* The order in which spz_circuit_execute would apply `ops` (host only):
+ * order[k] is the index of the k-th applied op and pass[k] the pass (kernel
+ * launch) that applies it; skipped ops do not appear.  *count receives the
+ * number of entries; at most `capacity` are written. */
+int spz_plan_schedule(uint32_t n, const spz_op* ops, size_t nops, uint32_t flags, uint32_t* order,
+                      uint32_t* pass, size_t capacity, size_t* count);
+
 /* iqft(&mut State, targets) (spinoza/src/core.rs:184-191). */
 int spz_iqft(spz_state_t h, const uint32_t* targets, uint32_t ntargets);
 

@@ -108,6 +108,8 @@ SIGNATURES = [
     ("spz_circuit_execute", c_int, [c_void_p, c_void_p, c_size_t, POINTER(spz_tracker), c_uint32,
                                     POINTER(spz_exec_stats)]),
     ("spz_plan_stats", c_int, [c_uint32, c_void_p, c_size_t, c_uint32, POINTER(spz_exec_stats)]),
+    ("spz_plan_schedule", c_int, [c_uint32, c_void_p, c_size_t, c_uint32, c_void_p, c_void_p, c_size_t,
+                                  POINTER(c_size_t)]),
     ("spz_iqft", c_int, [c_void_p, c_void_p, c_uint32]),
     ("spz_measure_qubit", c_int, [c_void_p, c_uint32, c_int, c_int, c_double, POINTER(c_uint8), POINTER(c_double)]),
     ("spz_prob0", c_int, [c_void_p, c_uint32, POINTER(c_double)]),

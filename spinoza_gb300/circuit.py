@@ -266,6 +266,20 @@ class QuantumCircuit:
                                                 byref(self.qubit_tracker.c), flags, byref(self.last_stats)))
 
 
+def plan_schedule(n: int, ops: np.ndarray, fused: bool = True) -> tuple[np.ndarray, np.ndarray]:
+    """(order, pass): the op indices in the order the executor applies them, and
+    the pass (kernel launch) of each (host only, no GPU)."""
+    ops = np.ascontiguousarray(ops, dtype=nat.OP_DTYPE)
+    flags = nat.EXEC_DEFAULT if fused else nat.EXEC_UNFUSED
+    cap = len(ops)
+    order = np.zeros(cap, dtype=np.uint32)
+    passes = np.zeros(cap, dtype=np.uint32)
+    count = nat.c_size_t()
+    nat.check(nat.lib().spz_plan_schedule(int(n), nat.ptr(ops), len(ops), flags, nat.ptr(order), nat.ptr(passes),
+                                          cap, byref(count)))
+    return order[: count.value], passes[: count.value]
+
+
 def plan_stats(n: int, ops: np.ndarray, fused: bool = True) -> dict:
     """How the executor would fuse `ops` on n qubits (host only, no GPU)."""
     st = nat.spz_exec_stats()

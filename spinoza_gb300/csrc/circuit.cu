@@ -12,9 +12,8 @@
 //
 // Exactness: each gate's per-pair arithmetic is the plain kernel's (the
 // reference's own operations).  The planner keeps program order except where a
-// swap of two gates is bit-exact: they commute on disjoint non-diagonal qubits
-// and one of them only moves or negates amplitudes (X, Y, Z, SWAP and their
-// controlled forms).  So a fused run is bit-identical to the sequential one.
+// swap of two gates is bit-exact (see ExactClass below).  So a fused run is
+// bit-identical to the sequential one.
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -167,8 +166,26 @@ __global__ void __launch_bounds__(kTileThreads) tile_kernel(PassArgs A) {
 // ------------------------------------------------------------ planner
 namespace {
 
-inline bool arithmetic_free(int kind) {
-  return kind == SPZ_GATE_X || kind == SPZ_GATE_Y || kind == SPZ_GATE_Z || kind == SPZ_GATE_SWAP;
+// Exact-commutation classes.  Two gates that commute mathematically (disjoint
+// non-diagonal qubits) also commute bit for bit when one of them only moves or
+// negates amplitudes (X, Z, SWAP: rounding is sign-symmetric), or when one is
+// Y (moves and multiplies by +-i) and the other's arithmetic treats real and
+// imaginary parts alike (H, RX, RY, and the moves).  P, RZ and U use FMAs whose
+// rounding differs between the real and imaginary parts, so G(i z) != i G(z)
+// in the last bit; two arithmetic gates never swap.
+enum ExactClass { EC_PERM = 0, EC_Y = 1, EC_ICOV = 2, EC_FMA = 3 };
+
+inline int exact_class(int kind) {
+  switch (kind) {
+    case SPZ_GATE_X:
+    case SPZ_GATE_Z:
+    case SPZ_GATE_SWAP: return EC_PERM;
+    case SPZ_GATE_Y: return EC_Y;
+    case SPZ_GATE_H:
+    case SPZ_GATE_RX:
+    case SPZ_GATE_RY: return EC_ICOV;
+    default: return EC_FMA;  // P, RZ, U
+  }
 }
 
 // Qubits a gate acts on non-diagonally (targets of pair gates, SWAP qubits)
@@ -201,7 +218,7 @@ std::vector<PlannedPass> plan(const std::vector<GateApp>& gates, uint32_t n, int
     int nl = __builtin_popcountll(L);
     std::vector<GateApp> deferred;
     uint64_t def_nd = 0, def_d = 0;
-    bool def_arith = false;
+    bool def_y = false, def_icov = false, def_fma = false;  // classes present among deferred gates
     const size_t lookahead = 4096;
     size_t i = 0;
     for (; i < remaining.size(); ++i) {
@@ -209,7 +226,10 @@ std::vector<PlannedPass> plan(const std::vector<GateApp>& gates, uint32_t n, int
       if (deferred.size() > lookahead) break;
       const uint64_t nd = nd_mask(g), d = d_mask(g);
       const bool commutes = (nd & (def_nd | def_d)) == 0 && (d & def_nd) == 0;
-      const bool exact_ok = arithmetic_free(g.kind) || !def_arith;
+      const int ec = exact_class(g.kind);
+      const bool exact_ok = ec == EC_PERM || (ec == EC_Y && !def_fma) ||
+                            (ec == EC_ICOV && !def_icov && !def_fma) ||
+                            (ec == EC_FMA && !def_icov && !def_fma && !def_y);
       bool take = false;
       if (deferred.empty() || (commutes && exact_ok)) {
         const uint64_t need = nd & ~L;
@@ -226,7 +246,9 @@ std::vector<PlannedPass> plan(const std::vector<GateApp>& gates, uint32_t n, int
         deferred.push_back(g);
         def_nd |= nd;
         def_d |= d;
-        def_arith |= !arithmetic_free(g.kind);
+        def_y |= ec == EC_Y;
+        def_icov |= ec == EC_ICOV;
+        def_fma |= ec == EC_FMA;
       }
     }
     for (; i < remaining.size(); ++i) deferred.push_back(remaining[i]);
@@ -542,7 +564,8 @@ int execute(spz_state_t h, const spz_op* ops, size_t nops, spz_tracker* tracker,
 }
 
 // Plan without executing (host only): fills the counters run_gates would.
-int plan_stats(uint32_t n, const spz_op* ops, size_t nops, uint32_t flags, spz_exec_stats* st) {
+int plan_stats(uint32_t n, const spz_op* ops, size_t nops, uint32_t flags, spz_exec_stats* st,
+               std::vector<uint32_t>* order = nullptr, std::vector<uint32_t>* pass_of = nullptr) {
   spz_state_s fake;
   fake.n = n;
   fake.N = 1ull << n;
@@ -552,6 +575,10 @@ int plan_stats(uint32_t n, const spz_op* ops, size_t nops, uint32_t flags, spz_e
     if (seg.empty()) return;
     if (flags & SPZ_EXEC_UNFUSED) {
       for (const GateApp& g : seg) {
+        if (order) {
+          order->push_back((uint32_t)g.src);
+          pass_of->push_back((uint32_t)st->passes);
+        }
         st->passes++;
         st->bytes_moved += gate_algorithmic_bytes(n, g);
       }
@@ -559,6 +586,11 @@ int plan_stats(uint32_t n, const spz_op* ops, size_t nops, uint32_t flags, spz_e
       const int k = std::min<int>((int)n, kTileMaxK);
       const int c = std::min<int>(kTileLowBits, k);
       for (const PlannedPass& P : plan(seg, n, k, c)) {
+        if (order)
+          for (const GateApp& g : P.gates) {
+            order->push_back((uint32_t)g.src);
+            pass_of->push_back((uint32_t)st->passes);
+          }
         st->passes++;
         if (P.gates.size() > 1) {
           st->tile_passes++;
@@ -578,6 +610,10 @@ int plan_stats(uint32_t n, const spz_op* ops, size_t nops, uint32_t flags, spz_e
       if (!((tr.measured >> op.target) & 1)) {
         flush();
         tr.measured |= 1ull << op.target;  // outcome unknown while planning: assume 0
+        if (order) {
+          order->push_back((uint32_t)i);
+          pass_of->push_back((uint32_t)st->passes);
+        }
         st->passes += 2;
       }
       continue;
@@ -587,6 +623,7 @@ int plan_stats(uint32_t n, const spz_op* ops, size_t nops, uint32_t flags, spz_e
     int rc = op_to_app(&fake, op, tr, &skip, &a);
     if (rc) return rc;
     if (skip) continue;
+    a.src = (int64_t)i;
     seg.push_back(a);
     st->gates++;
     st->algorithmic_bytes += gate_algorithmic_bytes(n, a);
@@ -616,6 +653,23 @@ int spz_plan_stats(uint32_t n, const spz_op* ops, size_t nops, uint32_t flags, s
   if (n == 0 || n > kMaxQubits) return fail(SPZ_ERR_INVALID_ARGUMENT, "n out of range");
   std::memset(stats, 0, sizeof(*stats));
   return plan_stats(n, ops, nops, flags, stats);
+}
+
+int spz_plan_schedule(uint32_t n, const spz_op* ops, size_t nops, uint32_t flags, uint32_t* order, uint32_t* pass,
+                      size_t capacity, size_t* count) {
+  if (!count || (capacity && (!order || !pass))) return fail(SPZ_ERR_NULL, "NULL argument");
+  if (nops && !ops) return fail(SPZ_ERR_NULL, "ops is NULL");
+  if (n == 0 || n > kMaxQubits) return fail(SPZ_ERR_INVALID_ARGUMENT, "n out of range");
+  spz_exec_stats st{};
+  std::vector<uint32_t> o, p;
+  int rc = plan_stats(n, ops, nops, flags, &st, &o, &p);
+  if (rc) return rc;
+  *count = o.size();
+  for (size_t i = 0; i < o.size() && i < capacity; ++i) {
+    order[i] = o[i];
+    pass[i] = p[i];
+  }
+  return SPZ_OK;
 }
 
 // core.rs:184-191: for j = len-1 .. 0: H(targets[j]); for k = j-1 .. 0:

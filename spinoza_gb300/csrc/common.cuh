@@ -116,6 +116,7 @@ struct GateApp {
   uint64_t ones;     // controls that must read 1
   uint64_t zeros;    // controls that must read 0
   Coef c;
+  int64_t src = -1;  // index of the circuit op it came from (planning reports)
 };
 
 // Validate and build a GateApp (returns a status).

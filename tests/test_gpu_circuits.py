@@ -155,7 +155,8 @@ def test_mid_circuit_measurement_and_classical_control(gpu):
         g, gtr, _ = _run_gpu(n, ops, init)
         o, otr = _run_oracle(ops, init)
         assert gtr == otr
-        _compare(g, o)
+        # the collapse scale 1/sqrt(prob0) comes from a sum in a different order
+        _compare(g, o, exact=False)
 
 
 def test_reference_circuit_tests(gpu):

@@ -110,6 +110,55 @@ def test_planner_fuses_brickwork(native):
     assert st["algorithmic_bytes"] == layers * (n * 32 + (n - 1) * 16) << n
 
 
+def random_ops(n, ngates, seed):
+    """Every gate kind with none / single / ones / mixed controls."""
+    r = np.random.default_rng(seed)
+    ops = np.zeros(ngates, dtype=nat.OP_DTYPE)
+    kinds = [nat.H, nat.X, nat.Y, nat.Z, nat.P, nat.RX, nat.RY, nat.RZ, nat.U, nat.SWAP]
+    for i in range(ngates):
+        k = int(r.choice(kinds))
+        q = r.permutation(n)
+        nc = int(r.integers(0, 4))
+        ctrls = [int(c) for c in q[2:2 + nc]]
+        ck = [nat.CONTROLS_NONE, nat.CONTROLS_SINGLE, nat.CONTROLS_ONES, nat.CONTROLS_ONES][nc]
+        zeros = 0
+        if nc >= 2 and r.random() < 0.5:
+            ck, zeros = nat.CONTROLS_MIXED, 1 << ctrls[0]
+        ops[i] = ((k, int(q[0]), int(q[1]), 0, r.uniform(-math.pi, math.pi, 3)), int(q[0]), ck,
+                  sum(1 << c for c in ctrls), zeros)
+    return ops
+
+
+@pytest.mark.parametrize("n", [5, 9, 13, 15])
+@pytest.mark.parametrize("seed", range(4))
+def test_planner_reordering_is_bit_exact(native, n, seed):
+    """Replaying the fused schedule gate by gate through the oracle gives the
+    sequential result bit for bit: the planner only swaps exactly-commuting gates."""
+    ops = random_ops(n, 200, 1000 * n + seed)
+    order, passes = circuit.plan_schedule(n, ops)
+    assert sorted(order.tolist()) == list(range(len(ops)))
+    assert np.all(np.diff(passes.astype(np.int64)) >= 0)
+    init = rng.uniform_state(n, seed)
+    a = [x.copy() for x in init]
+    oracle.execute(ops, *a)
+    b = [x.copy() for x in init]
+    for i in order:
+        oracle.execute(ops[i:i + 1], *b)
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def test_planner_schedule_brickwork_and_qft_bit_exact(native):
+    for n, ops in [(14, brickwork_ops(14, 3)), (14, qft_ops(14))]:
+        order, _ = circuit.plan_schedule(n, ops)
+        init = rng.uniform_state(n, 1)
+        a = [x.copy() for x in init]
+        oracle.execute(ops, *a)
+        b = [x.copy() for x in init]
+        for i in order:
+            oracle.execute(ops[i:i + 1], *b)
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
 def test_planner_measurement_is_a_barrier(native):
     ops = np.zeros(3, dtype=nat.OP_DTYPE)
     ops[0] = ((nat.H, 0, 0, 0, (0, 0, 0)), 0, 0, 0, 0)
