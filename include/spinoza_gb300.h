@@ -228,6 +228,23 @@ int spz_qubit_expectation_value(spz_state_t h, uint32_t target, double* out);
 int spz_xyz_expectation_value(spz_state_t h, char observable, const uint32_t* targets,
                               uint32_t ntargets, double* out);
 
+/* Allocation-free form of spz_xyz_expectation_value.  It has no counterpart in
+ * the reference.  It is for callers that cannot call cudaMalloc: code that runs
+ * inside another framework's memory pool or arena, inside a CUDA-graph capture
+ * that must not allocate, or in a process with a fixed memory budget.  It takes
+ * the state as raw device arrays (2^n doubles each) instead of a handle, runs on
+ * `stream` (a cudaStream_t, NULL = default stream) and writes ntargets results
+ * to `out` (host or device memory); it synchronises `stream` before returning.
+ * Its scratch is a static 10 KiB device array that every GPU loading the library
+ * holds until exit, so at most SPZ_NOALLOC_MAX_TARGETS targets per call; more
+ * returns SPZ_ERR_INVALID_ARGUMENT.  The first call on a device looks up the
+ * array's address on that device: make it before any stream capture.  All calls
+ * share the array: calls that overlap on the GPU race and must be serialised. */
+#define SPZ_NOALLOC_MAX_TARGETS 64
+int spz_xyz_expectation_value_noalloc(const double* d_reals, const double* d_imags, uint32_t n,
+                                      char observable, const uint32_t* targets, uint32_t ntargets,
+                                      double* out, void* stream);
+
 /* A Pauli string coeff * X^x_mask Z^z_mask with Y on bits set in both masks
  * (Y = i X Z per qubit, the phase is accounted for). */
 typedef struct spz_pauli_term {

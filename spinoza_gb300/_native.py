@@ -115,6 +115,8 @@ SIGNATURES = [
     ("spz_prob0", c_int, [c_void_p, c_uint32, POINTER(c_double)]),
     ("spz_qubit_expectation_value", c_int, [c_void_p, c_uint32, POINTER(c_double)]),
     ("spz_xyz_expectation_value", c_int, [c_void_p, c_char, c_void_p, c_uint32, c_void_p]),
+    ("spz_xyz_expectation_value_noalloc", c_int, [c_void_p, c_void_p, c_uint32, c_char, c_void_p, c_uint32,
+                                                  c_void_p, c_void_p]),
     ("spz_pauli_expectation", c_int, [c_void_p, c_void_p, c_size_t, POINTER(c_double)]),
     ("spz_norm_sqr", c_int, [c_void_p, POINTER(c_double)]),
     ("spz_sample", c_int, [c_void_p, c_void_p, c_size_t, c_void_p]),
