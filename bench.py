@@ -76,7 +76,8 @@ class ClockSampler:
 
     FIELDS = ["index", "clocks.sm", "clocks.max.sm", "power.draw", "clocks_event_reasons.active",
               "clocks_event_reasons.hw_slowdown", "clocks_event_reasons.hw_thermal_slowdown",
-              "clocks_event_reasons.sw_thermal_slowdown", "clocks_event_reasons.sw_power_cap"]
+              "clocks_event_reasons.sw_thermal_slowdown", "clocks_event_reasons.sw_power_cap",
+              "clocks_event_reasons.hw_power_brake_slowdown", "utilization.gpu", "temperature.gpu"]
 
     def __init__(self, device: int):
         self.device = device
@@ -105,22 +106,28 @@ class ClockSampler:
             self.lines = []
 
     def summary(self) -> dict:
-        sm, mx, reasons = [], None, set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        sm, mx, reasons, masks, power, util, temp = [], None, set(), set(), [], [], []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap", "hw_power_brake"]
         for ln in self.lines:
             f = [x.strip() for x in ln.split(",")]
-            if len(f) < 9:
+            if len(f) < 12:
                 continue
             try:
                 sm.append(float(f[1]))
                 mx = float(f[2])
+                power.append(float(f[3]))
+                util.append(float(f[10]))
+                temp.append(float(f[11]))
             except ValueError:
                 continue
-            for name, val in zip(names, f[5:9]):
+            masks.add(f[4])
+            for name, val in zip(names, f[5:10]):
                 if val.lower().startswith("active"):
                     reasons.add(name)
-        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
-                "samples": len(sm)}
+        med = (lambda v: statistics.median(v) if v else None)
+        return {"sm_mhz": med(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm),
+                "active_masks": sorted(masks), "power_w_median": med(power), "util_pct_median": med(util),
+                "temp_c_max": max(temp) if temp else None}
 
 
 def profile_traffic(kernel_file: str):
@@ -259,6 +266,7 @@ def gpu_arm(args) -> None:
                                                 flags, nat.byref(st)))
         return st
 
+    fma_rate_before = core.fp64_fma_rate()
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -290,7 +298,8 @@ def gpu_arm(args) -> None:
     tile_avg_ms = tile_ms / max(1, tile_launches)
     achieved = (32 * N) / (tile_avg_ms / 1e3) / 1e9
     traffic = profile_traffic("tile_kernel_brickwork30.txt")
-    fma_rate = core.fp64_fma_rate()
+    fma_rate_after = core.fp64_fma_rate()
+    fma_rate = max(fma_rate_before, fma_rate_after)
     fp64_achieved = fp64_ops / ((tile_ms + plain_ms) / 1e3)
 
     # end to end: host (pinned) |0...0> in, execute, host result out
@@ -350,8 +359,10 @@ def gpu_arm(args) -> None:
                          "note": "achieved = 32 N bytes (one read + one write of the state) per tile pass / mean "
                                  "tile-pass time; the tile passes are FP64-issue bound, see fp64"},
             "fp64": {"achieved": fp64_achieved, "peak": fma_rate, "unit": "FP64 instr/s", "frac": fp64_achieved / fma_rate,
+                     "peak_before": fma_rate_before, "peak_after": fma_rate_after,
                      "note": "FP64-pipe instructions the gates need / device time of the passes; peak = DFMA issue "
-                             "rate measured live on this GPU (spz_probe_fp64_fma_rate)"},
+                             "rate measured live on this GPU before and after the timed region "
+                             "(spz_probe_fp64_fma_rate), the larger of the two"},
             "cpu_baseline": cpu,
             "e2e": e2e,
             "gpu_launches": int(launches),

@@ -280,6 +280,49 @@ int spz_adjoint_gradient(spz_state_t h, const spz_op* ops, size_t nops,
                          const spz_pauli_term* terms, size_t nterms, double* energy,
                          double* grad);
 
+/* ---------------------------------------------------------------- batching */
+/* Many independent parameterised circuits of uneven qubit counts, each with its
+ * own Pauli-sum observable: E_i = <0|U_i(theta)^dagger H_i U_i(theta)|0> and
+ * dE_i/dtheta for all of them in one persistent launch, replayed as a CUDA
+ * graph.  Instances of up to tile_qubits qubits run entirely in shared memory;
+ * larger ones stream tiles through per-CTA workspace.  No reference
+ * counterpart (new form). */
+typedef struct spz_batch_s* spz_batch_t;
+
+typedef struct spz_batch_instance {
+  uint32_t n;             /* qubits (1..30)                                   */
+  uint32_t nops;          /* ops of this instance                             */
+  uint32_t nparams;       /* parameters of this instance                      */
+  uint32_t nterms;        /* Pauli terms of this instance's observable        */
+  uint64_t op_offset;     /* first op in `ops`                                */
+  uint64_t param_offset;  /* first entry in param_index / theta / grads       */
+  uint64_t term_offset;   /* first term in `terms`                            */
+} spz_batch_instance;
+
+typedef struct spz_batch_config {
+  int32_t tile_qubits;    /* local qubits per shared-memory tile, 4..12 (0 = 12) */
+  int32_t threads;        /* threads per CTA, multiple of 32 in 64..1024 (0 = 512) */
+  int32_t reserved[2];
+} spz_batch_config;
+
+typedef struct spz_batch_stats {
+  uint64_t instances, resident_instances;
+  uint64_t forward_passes, hamiltonian_passes, backward_passes;
+  uint64_t ctas, workspace_bytes;
+  int32_t tile_qubits, threads;
+} spz_batch_stats;
+
+/* Plan and upload a batch.  param_index[param_offset + j] is the op (relative to
+ * the instance's op_offset) whose angle p[0] is parameter j; only P, RX, RY and
+ * RZ angles can be parameters.  Ops may not contain M or BitFlipNoise. */
+int spz_batch_create(const spz_batch_instance* instances, size_t ninstances, const spz_op* ops,
+                     const uint32_t* param_index, const spz_pauli_term* terms,
+                     const spz_batch_config* config, spz_batch_t* out);
+/* theta[param_offset + j]: angles (host); energies[i] and grads[param_offset + j]: outputs (host). */
+int spz_batch_run(spz_batch_t b, const double* theta, double* energies, double* grads);
+int spz_batch_info(spz_batch_t b, spz_batch_stats* stats);
+int spz_batch_destroy(spz_batch_t b);
+
 /* ------------------------------------------------------------------ probes */
 /* Measured FP64 FMA issue rate of the current device (FMA/s): the second
  * roofline (beside HBM bandwidth) that bounds dense FP64 gate kernels. */

@@ -75,6 +75,25 @@ class spz_pauli_term(ctypes.Structure):
     _fields_ = [("coeff", c_double), ("x_mask", c_uint64), ("z_mask", c_uint64)]
 
 
+class spz_batch_instance(ctypes.Structure):
+    _fields_ = [("n", c_uint32), ("nops", c_uint32), ("nparams", c_uint32), ("nterms", c_uint32),
+                ("op_offset", c_uint64), ("param_offset", c_uint64), ("term_offset", c_uint64)]
+
+
+class spz_batch_config(ctypes.Structure):
+    _fields_ = [("tile_qubits", c_int32), ("threads", c_int32), ("reserved", c_int32 * 2)]
+
+
+class spz_batch_stats(ctypes.Structure):
+    _fields_ = [("instances", c_uint64), ("resident_instances", c_uint64), ("forward_passes", c_uint64),
+                ("hamiltonian_passes", c_uint64), ("backward_passes", c_uint64), ("ctas", c_uint64),
+                ("workspace_bytes", c_uint64), ("tile_qubits", c_int32), ("threads", c_int32)]
+
+
+INSTANCE_DTYPE = np.dtype([("n", "<u4"), ("nops", "<u4"), ("nparams", "<u4"), ("nterms", "<u4"),
+                           ("op_offset", "<u8"), ("param_offset", "<u8"), ("term_offset", "<u8")])
+
+
 # numpy mirrors of the structs (for building large op lists without Python loops)
 GATE_DTYPE = np.dtype([("kind", "<i4"), ("q0", "<u4"), ("q1", "<u4"), ("pad_", "<u4"), ("p", "<f8", (3,))])
 OP_DTYPE = np.dtype([("gate", GATE_DTYPE), ("target", "<u4"), ("controls_kind", "<i4"),
@@ -122,6 +141,11 @@ SIGNATURES = [
     ("spz_sample", c_int, [c_void_p, c_void_p, c_size_t, c_void_p]),
     ("spz_adjoint_gradient", c_int, [c_void_p, c_void_p, c_size_t, c_void_p, c_size_t, c_void_p, c_size_t,
                                      POINTER(c_double), c_void_p]),
+    ("spz_batch_create", c_int, [c_void_p, c_size_t, c_void_p, c_void_p, c_void_p, POINTER(spz_batch_config),
+                                 POINTER(c_void_p)]),
+    ("spz_batch_run", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    ("spz_batch_info", c_int, [c_void_p, POINTER(spz_batch_stats)]),
+    ("spz_batch_destroy", c_int, [c_void_p]),
     ("spz_probe_fp64_fma_rate", c_int, [POINTER(c_double)]),
 ]
 

@@ -1,0 +1,883 @@
+// Batched variational workload: forward <H> and adjoint gradients of many
+// independent parameterised circuits of uneven qubit counts in ONE persistent
+// launch, replayed as a CUDA graph.  No reference counterpart (a new form built
+// on the gate path).
+//
+// Work split.  Each CTA takes whole instances from a global work counter
+// (largest first) and runs, for that instance:
+//   forward passes   psi = G_L ... G_1 |0>          (tiles of 2^k amplitudes)
+//   Hamiltonian      lam = H psi, E = Re<psi|lam>    (Pauli terms, tile passes)
+//   backward passes  per gate in reverse: the tile's part of <lam|K|psi>,
+//                    then G^dagger on both psi and lam (fused: one load of each)
+// An instance of n <= k qubits lives entirely in shared memory (no HBM traffic
+// beyond parameters in and energy / gradients out).  Larger instances stream
+// tiles through a per-CTA workspace in HBM (psi and lam, 2 x 16 B x 2^n), using
+// the same planner as the fused circuit executor.  A CTA never waits on another
+// CTA, so there is no inter-CTA synchronisation to bound.
+//
+// Determinism: one CTA per instance, tiles in a fixed order, fixed reduction
+// trees: results are identical from run to run.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "common.cuh"
+#include "gate_math.cuh"
+
+namespace spz {
+
+bool exactly_commuting_kinds(int a, int b);
+
+namespace {
+
+constexpr int kBatchMaxK = 12;
+constexpr int kBatchLowBits = 3;
+constexpr int kMaxPassParams = 256;  // gradient accumulators per backward pass
+constexpr uint64_t kWorkspaceBudget = 24ull << 30;  // HBM for streamed instances' psi and lam
+
+enum BPassKind { BP_FWD = 0, BP_HAM = 1, BP_BWD = 2 };
+enum BMode { BM_PAIR = 0, BM_DIAG_LOCAL = 1, BM_DIAG_GLOBAL = 2, BM_SWAP = 3 };
+enum BGrad { BG_NONE = -1, BG_X = 0, BG_Y = 1, BG_Z = 2, BG_P1 = 3 };
+
+struct BGate {
+  int32_t kind;
+  int32_t mode;
+  uint32_t tbit, tbit2, l_ones;
+  int32_t npos;
+  uint8_t pos[16];
+  uint64_t g_ones, g_zeros, g_tbit;
+  int32_t param;      // instance-relative parameter whose angle this gate uses (-1: fixed)
+  int32_t sign;       // +1: angle, -1: inverse gate (negated angle)
+  int32_t grad;       // backward: BGrad mode of the gradient taken before un-applying
+  int32_t gacc;       // backward: accumulator slot within the pass
+  Coef c;
+};
+
+struct HTerm {
+  double coeff;
+  uint64_t x_local;   // X-part as a mask of local bits
+  uint64_t x_global;  // X-part as a mask of qubits
+  uint64_t z_mask;    // Z-part as a mask of qubits
+  int32_t ny;         // number of Y factors (phase i^ny)
+  int32_t pad;
+};
+
+struct BPass {
+  uint32_t gate_begin, gate_count;
+  uint32_t term_begin, term_count;
+  int32_t kind, k, c, nhigh;
+  int32_t first;      // FWD: synthesise |0..0>; HAM: lambda starts at 0
+  int32_t nparams;    // BWD: accumulator slots used
+  uint8_t lpos[16];
+};
+
+struct BInst {
+  uint32_t n;
+  uint32_t pass_begin, npass;
+  int32_t resident;   // n <= k: the whole instance stays in shared memory
+  int64_t param_offset;
+  int32_t nparams;
+  int32_t pad;
+};
+
+struct BatchArgs {
+  const BInst* inst;
+  const uint32_t* order;
+  uint32_t ninst;
+  const BPass* passes;
+  const BGate* gates;
+  const HTerm* terms;
+  double* energies;
+  double* grads;
+  double* workspace;      // per CTA: psi_re, psi_im, lam_re, lam_im of 2^ws_qubits each
+  uint32_t ws_qubits;
+  unsigned int* counter;
+  int kmax;
+};
+
+__device__ __forceinline__ double bsum(double v, double* red) {
+  for (int off = 16; off > 0; off >>= 1) v = dadd(v, __shfl_down_sync(0xffffffffu, v, off));
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) red[warp] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (warp == 0) {
+    r = lane < (int)(blockDim.x >> 5) ? red[lane] : 0.0;
+    for (int off = 16; off > 0; off >>= 1) r = dadd(r, __shfl_down_sync(0xffffffffu, r, off));
+  }
+  __syncthreads();
+  return r;  // thread 0
+}
+
+template <int KIND>
+__device__ __forceinline__ void b_pair(const BGate& g, double* re, double* im, uint32_t nw) {
+  for (uint32_t m = threadIdx.x; m < nw; m += blockDim.x) {
+    const uint32_t s0 = (uint32_t)deposit(m, g.pos, g.npos) | g.l_ones;
+    const uint32_t s1 = s0 | g.tbit;
+    double a = re[s0], b = im[s0], c = re[s1], d = im[s1];
+    gate_pair<KIND>(g.c, a, b, c, d);
+    re[s0] = a; im[s0] = b; re[s1] = c; im[s1] = d;
+  }
+}
+
+template <int KIND>
+__device__ __forceinline__ void b_diag(const BGate& g, double* re, double* im, uint32_t nw, int gone) {
+  for (uint32_t m = threadIdx.x; m < nw; m += blockDim.x) {
+    const uint32_t e = (uint32_t)deposit(m, g.pos, g.npos) | g.l_ones;
+    const bool one = gone >= 0 ? gone != 0 : (e & g.tbit) != 0;
+    double r = re[e], i = im[e];
+    gate_diag<KIND>(g.c, one, r, i);
+    re[e] = r; im[e] = i;
+  }
+}
+
+// Apply one gate to a tile (caller checked the non-local control predicate).
+__device__ void b_apply(const BGate& g, uint64_t base, double* re, double* im, uint32_t T) {
+  const uint32_t nw = T >> g.npos;
+  switch (g.mode) {
+    case BM_PAIR:
+      switch (g.kind) {
+        case SPZ_GATE_H: b_pair<SPZ_GATE_H>(g, re, im, nw); break;
+        case SPZ_GATE_X: b_pair<SPZ_GATE_X>(g, re, im, nw); break;
+        case SPZ_GATE_Y: b_pair<SPZ_GATE_Y>(g, re, im, nw); break;
+        case SPZ_GATE_RX: b_pair<SPZ_GATE_RX>(g, re, im, nw); break;
+        case SPZ_GATE_RY: b_pair<SPZ_GATE_RY>(g, re, im, nw); break;
+        default: b_pair<SPZ_GATE_U>(g, re, im, nw); break;
+      }
+      break;
+    case BM_DIAG_LOCAL:
+    case BM_DIAG_GLOBAL: {
+      int gone = -1;
+      if (g.mode == BM_DIAG_GLOBAL) {
+        gone = (base & g.g_tbit) ? 1 : 0;
+        if (!gone && g.kind != SPZ_GATE_RZ) break;
+      }
+      switch (g.kind) {
+        case SPZ_GATE_Z: b_diag<SPZ_GATE_Z>(g, re, im, nw, gone); break;
+        case SPZ_GATE_P: b_diag<SPZ_GATE_P>(g, re, im, nw, gone); break;
+        default: b_diag<SPZ_GATE_RZ>(g, re, im, nw, gone); break;
+      }
+      break;
+    }
+    default:
+      for (uint32_t m = threadIdx.x; m < nw; m += blockDim.x) {
+        const uint32_t b0 = (uint32_t)deposit(m, g.pos, g.npos) | g.l_ones;
+        const uint32_t i = b0 | g.tbit2, j = b0 | g.tbit;
+        const double r = re[i], q = im[i];
+        re[i] = re[j]; im[i] = im[j];
+        re[j] = r; im[j] = q;
+      }
+  }
+}
+
+// This thread's share of Im<lam| Pi sigma |psi> over the gate's amplitudes in
+// the tile.  X and Y generators pair s0 with s1 (the target is local); the
+// diagonal generators (Z for RZ, |1><1| for P) are elementwise,
+// sum over x of +-Im(conj(lam_x) psi_x), with the target bit read from the
+// element or, for a non-local target, from the tile base.
+__device__ double b_grad_part(const BGate& g, uint64_t base, const double* pr, const double* pi,
+                              const double* lr, const double* li, uint32_t T) {
+  const uint32_t nw = T >> g.npos;
+  double acc = 0.0;
+  if (g.mode != BM_PAIR) {
+    const int gone = g.mode == BM_DIAG_GLOBAL ? ((base & g.g_tbit) ? 1 : 0) : -1;
+    if (g.grad == BG_P1 && gone == 0) return 0.0;
+    for (uint32_t m = threadIdx.x; m < nw; m += blockDim.x) {
+      const uint32_t e = (uint32_t)deposit(m, g.pos, g.npos) | g.l_ones;
+      const bool one = gone >= 0 ? gone != 0 : (e & g.tbit) != 0;
+      if (g.grad == BG_P1 && !one) continue;
+      const double v = dfma(lr[e], pi[e], dmul(dneg(li[e]), pr[e]));  // Im(conj(lam) psi)
+      acc = (g.grad == BG_Z && one) ? dsub(acc, v) : dadd(acc, v);
+    }
+    return acc;
+  }
+  for (uint32_t m = threadIdx.x; m < nw; m += blockDim.x) {
+    const uint32_t s0 = (uint32_t)deposit(m, g.pos, g.npos) | g.l_ones;
+    const uint32_t s1 = s0 | g.tbit;
+    const double a = pr[s0], b = pi[s0], c = pr[s1], d = pi[s1];
+    const double p = lr[s0], q = li[s0], r = lr[s1], s = li[s1];
+    double v;
+    switch (g.grad) {
+      case BG_X: v = dadd(dfma(p, d, dmul(dneg(q), c)), dfma(r, b, dmul(dneg(s), a))); break;
+      case BG_Y: v = dsub(dfma(r, a, dmul(s, b)), dfma(p, c, dmul(q, d))); break;
+      case BG_Z: v = dsub(dfma(p, b, dmul(dneg(q), a)), dfma(r, d, dmul(dneg(s), c))); break;
+      default: v = dfma(r, d, dmul(dneg(s), c)); break;
+    }
+    acc = dadd(acc, v);
+  }
+  return acc;
+}
+
+__device__ __forceinline__ uint64_t b_global(uint64_t base, const uint64_t* rowoff, uint32_t e, int c) {
+  return base | rowoff[e >> c] | (e & ((1u << c) - 1));
+}
+
+__global__ void __launch_bounds__(1024) batch_kernel(BatchArgs A) {
+  extern __shared__ double sm[];
+  const uint32_t TMAX = 1u << A.kmax;
+  double* pr = sm;
+  double* pi = sm + TMAX;
+  double* lr = sm + 2 * TMAX;
+  double* li = sm + 3 * TMAX;
+  uint64_t* rowoff = reinterpret_cast<uint64_t*>(sm + 4 * TMAX);
+  double* red = sm + 4 * TMAX + (TMAX >> kBatchLowBits);
+  double* gacc = red + 64;
+  __shared__ unsigned int s_next;
+  __shared__ double s_energy;
+  const uint64_t wsN = 1ull << A.ws_qubits;
+  double* wpr = A.workspace ? A.workspace + (uint64_t)blockIdx.x * 4 * wsN : nullptr;
+  double* wpi = wpr ? wpr + wsN : nullptr;
+  double* wlr = wpr ? wpr + 2 * wsN : nullptr;
+  double* wli = wpr ? wpr + 3 * wsN : nullptr;
+
+  for (;;) {
+    if (threadIdx.x == 0) s_next = atomicAdd(A.counter, 1u);
+    __syncthreads();
+    const unsigned int q = s_next;
+    __syncthreads();
+    if (q >= A.ninst) break;
+    const BInst I = A.inst[A.order[q]];
+    if (threadIdx.x == 0) s_energy = 0.0;
+    __syncthreads();
+    for (uint32_t pidx = 0; pidx < I.npass; ++pidx) {
+      const BPass& P = A.passes[I.pass_begin + pidx];
+      const int K = P.k, C = P.c;
+      const uint32_t T = 1u << K;
+      const uint64_t ntiles = 1ull << (I.n - K);
+      if (!I.resident) {
+        for (uint32_t r = threadIdx.x; r < (1u << P.nhigh); r += blockDim.x) {
+          uint64_t off = 0;
+          for (int j = 0; j < P.nhigh; ++j)
+            if ((r >> j) & 1) off |= 1ull << P.lpos[C + j];
+          rowoff[r] = off;
+        }
+      }
+      if (P.kind == BP_BWD)
+        for (int j = threadIdx.x; j < P.nparams; j += blockDim.x) gacc[j] = 0.0;
+      __syncthreads();
+      for (uint64_t tile = 0; tile < ntiles; ++tile) {
+        const uint64_t base = I.resident ? 0 : deposit(tile, P.lpos, K);
+        // ---- load
+        if (P.kind == BP_FWD && P.first) {
+          for (uint32_t e = threadIdx.x; e < T; e += blockDim.x) {
+            const uint64_t gi = I.resident ? e : b_global(base, rowoff, e, C);
+            pr[e] = gi == 0 ? 1.0 : 0.0;
+            pi[e] = 0.0;
+          }
+        } else if (!I.resident) {
+          for (uint32_t e2 = threadIdx.x; e2 < T / 2; e2 += blockDim.x) {
+            const uint32_t e = 2 * e2;
+            const uint64_t gi = b_global(base, rowoff, e, C);
+            *reinterpret_cast<double2*>(pr + e) = *reinterpret_cast<const double2*>(wpr + gi);
+            *reinterpret_cast<double2*>(pi + e) = *reinterpret_cast<const double2*>(wpi + gi);
+            if (P.kind == BP_BWD || (P.kind == BP_HAM && !P.first)) {
+              *reinterpret_cast<double2*>(lr + e) = *reinterpret_cast<const double2*>(wlr + gi);
+              *reinterpret_cast<double2*>(li + e) = *reinterpret_cast<const double2*>(wli + gi);
+            }
+          }
+        }
+        __syncthreads();
+        // ---- work
+        if (P.kind == BP_FWD) {
+          for (uint32_t gi = 0; gi < P.gate_count; ++gi) {
+            const BGate& g = A.gates[P.gate_begin + gi];
+            if ((base & g.g_ones) != g.g_ones || (base & g.g_zeros) != 0) continue;
+            b_apply(g, base, pr, pi, T);
+            __syncthreads();
+          }
+        } else if (P.kind == BP_HAM) {
+          double eacc = 0.0;
+          for (uint32_t e = threadIdx.x; e < T; e += blockDim.x) {
+            const uint64_t gx = I.resident ? e : b_global(base, rowoff, e, C);
+            double dr = 0.0, di = 0.0;
+            for (uint32_t k = 0; k < P.term_count; ++k) {
+              const HTerm& h = A.terms[P.term_begin + k];
+              const uint32_t ye = e ^ (uint32_t)h.x_local;
+              const uint64_t gy = gx ^ h.x_global;
+              double cf = (__popcll(gy & h.z_mask) & 1) ? dneg(h.coeff) : h.coeff;
+              const int ny = h.ny & 3;
+              if (ny >= 2) cf = dneg(cf);
+              const double yr = pr[ye], yi = pi[ye];
+              if (ny & 1) {  // i * cf * psi_y
+                dr = dfma(dneg(cf), yi, dr);
+                di = dfma(cf, yr, di);
+              } else {
+                dr = dfma(cf, yr, dr);
+                di = dfma(cf, yi, di);
+              }
+            }
+            eacc = dadd(eacc, dfma(pr[e], dr, dmul(pi[e], di)));
+            if (P.first) {
+              lr[e] = dr;
+              li[e] = di;
+            } else {
+              lr[e] = dadd(lr[e], dr);
+              li[e] = dadd(li[e], di);
+            }
+          }
+          const double es = bsum(eacc, red);
+          if (threadIdx.x == 0) s_energy = dadd(s_energy, es);
+        } else {  // BP_BWD
+          for (uint32_t gi = 0; gi < P.gate_count; ++gi) {
+            const BGate& g = A.gates[P.gate_begin + gi];
+            if ((base & g.g_ones) != g.g_ones || (base & g.g_zeros) != 0) continue;
+            if (g.grad != BG_NONE) {
+              const double part = bsum(b_grad_part(g, base, pr, pi, lr, li, T), red);
+              if (threadIdx.x == 0) gacc[g.gacc] = dadd(gacc[g.gacc], part);
+            }
+            b_apply(g, base, pr, pi, T);
+            b_apply(g, base, lr, li, T);
+            __syncthreads();
+          }
+        }
+        __syncthreads();
+        // ---- store
+        if (!I.resident) {
+          const bool store_psi = P.kind != BP_HAM;
+          const bool store_lam = P.kind != BP_FWD;
+          for (uint32_t e2 = threadIdx.x; e2 < T / 2; e2 += blockDim.x) {
+            const uint32_t e = 2 * e2;
+            const uint64_t gi = b_global(base, rowoff, e, C);
+            if (store_psi) {
+              *reinterpret_cast<double2*>(wpr + gi) = *reinterpret_cast<const double2*>(pr + e);
+              *reinterpret_cast<double2*>(wpi + gi) = *reinterpret_cast<const double2*>(pi + e);
+            }
+            if (store_lam) {
+              *reinterpret_cast<double2*>(wlr + gi) = *reinterpret_cast<const double2*>(lr + e);
+              *reinterpret_cast<double2*>(wli + gi) = *reinterpret_cast<const double2*>(li + e);
+            }
+          }
+        }
+        __syncthreads();
+      }
+      if (P.kind == BP_BWD) {
+        for (uint32_t gi = threadIdx.x; gi < P.gate_count; gi += blockDim.x) {
+          const BGate& g = A.gates[P.gate_begin + gi];
+          if (g.grad != BG_NONE) {
+            const double v = gacc[g.gacc];
+            A.grads[I.param_offset + g.param] = g.grad == BG_P1 ? dmul(-2.0, v) : v;
+          }
+        }
+        __syncthreads();
+      }
+    }
+    if (threadIdx.x == 0) A.energies[A.order[q]] = s_energy;
+    __syncthreads();
+  }
+}
+
+// Coefficients of every parameterised gate from the current angles.
+struct CoefJob {
+  uint32_t gate;
+  int32_t kind;
+  int64_t theta_index;
+  int32_t sign;
+  int32_t pad;
+};
+
+__global__ void batch_coef_kernel(BGate* gates, const CoefJob* jobs, uint32_t njobs, const double* theta) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= njobs) return;
+  const CoefJob j = jobs[i];
+  const double th = j.sign > 0 ? theta[j.theta_index] : -theta[j.theta_index];
+  Coef& c = gates[j.gate].c;
+  double s, co;
+  switch (j.kind) {
+    case SPZ_GATE_P:
+      sincos(th, &s, &co);
+      c.sn = s; c.cs = co; c.nsn = -s;
+      break;
+    case SPZ_GATE_RX:
+      sincos(th * 0.5, &s, &co);
+      c.cs = co; c.nsn = -s; c.sn = s;
+      break;
+    case SPZ_GATE_RY:
+      sincos(th * 0.5, &s, &co);
+      c.sn = s; c.cs = co; c.nsn = -s;
+      break;
+    default:  // RZ
+      sincos(th * 0.5, &s, &co);
+      c.d0re = co; c.d0im = -s; c.d1re = co; c.d1im = s;
+      break;
+  }
+}
+
+BGate to_bgate(const GateApp& g, const std::vector<int>& local) {
+  int where[64];
+  for (int q = 0; q < 64; ++q) where[q] = -1;
+  for (size_t j = 0; j < local.size(); ++j) where[local[j]] = (int)j;
+  BGate t{};
+  t.kind = g.kind;
+  t.c = g.c;
+  t.param = -1;
+  t.sign = 1;
+  t.grad = BG_NONE;
+  uint32_t l_ones = 0, l_zeros = 0;
+  for (int q = 0; q < 64; ++q) {
+    const uint64_t b = 1ull << q;
+    if (g.ones & b) {
+      if (where[q] >= 0) l_ones |= 1u << where[q]; else t.g_ones |= b;
+    }
+    if (g.zeros & b) {
+      if (where[q] >= 0) l_zeros |= 1u << where[q]; else t.g_zeros |= b;
+    }
+  }
+  uint32_t special = l_ones | l_zeros;
+  if (g.kind == SPZ_GATE_SWAP) {
+    t.mode = BM_SWAP;
+    t.tbit = 1u << where[g.target];
+    t.tbit2 = 1u << where[g.target2];
+    special |= t.tbit | t.tbit2;
+  } else if (is_diagonal(g.kind)) {
+    if (where[g.target] >= 0) {
+      t.mode = BM_DIAG_LOCAL;
+      t.tbit = 1u << where[g.target];
+      if (g.kind != SPZ_GATE_RZ) {
+        special |= t.tbit;
+        l_ones |= t.tbit;
+      }
+    } else {
+      t.mode = BM_DIAG_GLOBAL;
+      t.g_tbit = 1ull << g.target;
+    }
+  } else {
+    t.mode = BM_PAIR;
+    t.tbit = 1u << where[g.target];
+    special |= t.tbit;
+  }
+  t.l_ones = l_ones;
+  for (int j = 0; j < 32; ++j)
+    if ((special >> j) & 1) t.pos[t.npos++] = (uint8_t)j;
+  return t;
+}
+
+spz_gate inverse_of(const spz_gate& g) {
+  spz_gate r = g;
+  switch (g.kind) {
+    case SPZ_GATE_P: case SPZ_GATE_RX: case SPZ_GATE_RY: case SPZ_GATE_RZ: r.p[0] = -g.p[0]; break;
+    case SPZ_GATE_U: r.p[0] = -g.p[0]; r.p[1] = -g.p[2]; r.p[2] = -g.p[1]; break;
+    default: break;
+  }
+  return r;
+}
+
+}  // namespace
+
+struct BatchImpl {
+  int device = 0;
+  int kmax = kBatchMaxK, threads = 512;
+  uint32_t ninst = 0;
+  uint64_t nparams_total = 0;
+  uint32_t ws_qubits = 0;
+  int grid = 0;
+  size_t smem = 0;
+  cudaStream_t stream = nullptr;
+  // device
+  BInst* d_inst = nullptr;
+  uint32_t* d_order = nullptr;
+  BPass* d_pass = nullptr;
+  BGate* d_gates = nullptr;
+  HTerm* d_terms = nullptr;
+  CoefJob* d_jobs = nullptr;
+  uint32_t njobs = 0;
+  double* d_theta = nullptr;
+  double* d_energy = nullptr;
+  double* d_grad = nullptr;
+  double* d_ws = nullptr;
+  unsigned int* d_counter = nullptr;
+  // pinned staging
+  double* h_theta = nullptr;
+  double* h_energy = nullptr;
+  double* h_grad = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  // plan statistics
+  uint64_t fwd_passes = 0, ham_passes = 0, bwd_passes = 0, resident = 0;
+};
+
+}  // namespace spz
+
+struct spz_batch_s : spz::BatchImpl {};
+
+namespace spz {
+namespace {
+
+void free_batch(spz_batch_t b) {
+  if (!b) return;
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  cudaFree(b->d_inst); cudaFree(b->d_order); cudaFree(b->d_pass); cudaFree(b->d_gates); cudaFree(b->d_terms);
+  cudaFree(b->d_jobs); cudaFree(b->d_theta); cudaFree(b->d_energy); cudaFree(b->d_grad); cudaFree(b->d_ws);
+  cudaFree(b->d_counter);
+  cudaFreeHost(b->h_theta); cudaFreeHost(b->h_energy); cudaFreeHost(b->h_grad);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+}
+
+template <typename T>
+int upload(T** dst, const std::vector<T>& src) {
+  const size_t bytes = std::max<size_t>(1, src.size()) * sizeof(T);
+  SPZ_CUDA(cudaMalloc((void**)dst, bytes));
+  if (!src.empty()) SPZ_CUDA(cudaMemcpy(*dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return SPZ_OK;
+}
+
+int build_batch(spz_batch_t b, const spz_batch_instance* inst, size_t ninst, const spz_op* ops,
+                const uint32_t* param_index, const spz_pauli_term* terms) {
+  std::vector<BInst> vinst(ninst);
+  std::vector<BPass> vpass;
+  std::vector<BGate> vgates;
+  std::vector<HTerm> vterms;
+  std::vector<CoefJob> jobs;
+  std::vector<double> cost(ninst);
+  uint64_t ptotal = 0;
+  uint32_t ws_qubits = 0;
+  for (size_t ii = 0; ii < ninst; ++ii) {
+    const spz_batch_instance& in = inst[ii];
+    const uint32_t n = in.n;
+    if (n == 0 || n > 30) return fail(SPZ_ERR_INVALID_ARGUMENT, "batch instance qubits must be in 1..30");
+    const int k = std::min<int>((int)n, b->kmax);
+    const int c = std::min<int>(kBatchLowBits, k);
+    // forward gate list (+ which op carries which parameter)
+    std::vector<int> param_of_op(in.nops, -1);
+    for (uint32_t j = 0; j < in.nparams; ++j) {
+      const uint32_t op = param_index[in.param_offset + j];
+      if (op >= in.nops) return fail(SPZ_ERR_INVALID_ARGUMENT, "batch param_index out of range");
+      if (param_of_op[op] >= 0) return fail(SPZ_ERR_INVALID_ARGUMENT, "an op carries two parameters");
+      const int kind = ops[in.op_offset + op].gate.kind;
+      if (kind != SPZ_GATE_RX && kind != SPZ_GATE_RY && kind != SPZ_GATE_RZ && kind != SPZ_GATE_P)
+        return fail(SPZ_ERR_UNSUPPORTED, "only P, RX, RY and RZ angles can be batch parameters");
+      param_of_op[op] = (int)j;
+    }
+    std::vector<GateApp> fwd;
+    std::vector<spz_gate> fwd_gate;
+    for (uint32_t o = 0; o < in.nops; ++o) {
+      const spz_op& op = ops[in.op_offset + o];
+      if (op.gate.kind == SPZ_GATE_M || op.gate.kind == SPZ_GATE_BITFLIP)
+        return fail(SPZ_ERR_UNSUPPORTED, "measurements and noise cannot be batched");
+      uint64_t ones = 0, zeros = 0;
+      if (op.controls_kind == SPZ_CONTROLS_MIXED) {
+        ones = op.controls & ~op.zeros;
+        zeros = op.zeros;
+      } else if (op.controls_kind != SPZ_CONTROLS_NONE) {
+        ones = op.controls;
+      }
+      GateApp a;
+      int rc = make_gate_app(n, op.gate, op.target, ones, zeros, &a);
+      if (rc) return rc;
+      a.src = o;
+      fwd.push_back(a);
+      fwd_gate.push_back(op.gate);
+    }
+    BInst& I = vinst[ii];
+    I.n = n;
+    I.pass_begin = (uint32_t)vpass.size();
+    I.resident = (int)n <= b->kmax;
+    I.param_offset = (int64_t)in.param_offset;
+    I.nparams = (int)in.nparams;
+    ptotal = std::max<uint64_t>(ptotal, in.param_offset + in.nparams);
+    if (!I.resident) ws_qubits = std::max<uint32_t>(ws_qubits, n);
+    // forward passes (a resident instance is one pass over all n qubits, in program order)
+    std::vector<int> all_local(n);
+    std::iota(all_local.begin(), all_local.end(), 0);
+    std::vector<PlannedPass> fp;
+    if (I.resident) {
+      if (!fwd.empty()) fp.push_back(PlannedPass{all_local, fwd});
+    } else {
+      fp = plan_passes(fwd, n, k, c);
+    }
+    std::vector<GateApp> applied;  // in the order the passes apply them
+    bool first = true;
+    for (const PlannedPass& P : fp) {
+      BPass bp{};
+      bp.kind = BP_FWD;
+      bp.k = (int)P.local.size();
+      bp.c = c;
+      bp.nhigh = bp.k - c;
+      bp.first = first;
+      first = false;
+      for (int j = 0; j < bp.k; ++j) bp.lpos[j] = (uint8_t)P.local[j];
+      bp.gate_begin = (uint32_t)vgates.size();
+      for (const GateApp& g : P.gates) {
+        BGate t = to_bgate(g, P.local);
+        const int pj = param_of_op[g.src];
+        if (pj >= 0) {
+          t.param = pj;
+          jobs.push_back(CoefJob{(uint32_t)vgates.size(), g.kind, (int64_t)in.param_offset + pj, 1, 0});
+        }
+        vgates.push_back(t);
+        applied.push_back(g);
+      }
+      bp.gate_count = (uint32_t)(vgates.size() - bp.gate_begin);
+      vpass.push_back(bp);
+      b->fwd_passes++;
+    }
+    if (fp.empty()) {  // no gates: one empty first pass to set |0...0>
+      BPass bp{};
+      bp.kind = BP_FWD; bp.k = k; bp.c = c; bp.nhigh = k - c; bp.first = 1;
+      for (int j = 0; j < k; ++j) bp.lpos[j] = (uint8_t)j;
+      bp.gate_begin = (uint32_t)vgates.size();
+      vpass.push_back(bp);
+    }
+    // Hamiltonian passes: diagonal terms in the first; X-type terms in passes
+    // whose local set covers their X bits.
+    std::vector<int> done(in.nterms, 0);
+    size_t remaining = in.nterms;
+    bool hfirst = true;
+    while (remaining > 0 || hfirst) {
+      uint64_t L = (c >= 64) ? ~0ull : ((1ull << c) - 1);
+      int nl = c;
+      std::vector<uint32_t> take;
+      for (uint32_t t = 0; t < in.nterms; ++t) {
+        if (done[t]) continue;
+        const spz_pauli_term& tm = terms[in.term_offset + t];
+        if (n < 64 && ((tm.x_mask | tm.z_mask) >> n) != 0)
+          return fail(SPZ_ERR_INVALID_ARGUMENT, "Pauli term acts on a qubit out of range");
+        const uint64_t need = tm.x_mask & ~L;
+        const int add = __builtin_popcountll(need);
+        if (nl + add <= k) {
+          L |= need;
+          nl += add;
+          take.push_back(t);
+        } else if (__builtin_popcountll(tm.x_mask) > k) {
+          return fail(SPZ_ERR_UNSUPPORTED, "Pauli term with more X/Y qubits than a tile holds");
+        }
+      }
+      for (int q = 0; q < (int)n && nl < k; ++q)
+        if (!((L >> q) & 1)) { L |= 1ull << q; nl++; }
+      std::vector<int> local;
+      for (int q = 0; q < (int)n; ++q)
+        if ((L >> q) & 1) local.push_back(q);
+      int where[64];
+      for (int q = 0; q < 64; ++q) where[q] = -1;
+      for (size_t j = 0; j < local.size(); ++j) where[local[j]] = (int)j;
+      BPass bp{};
+      bp.kind = BP_HAM;
+      bp.k = (int)local.size();
+      bp.c = c;
+      bp.nhigh = bp.k - c;
+      bp.first = hfirst;
+      hfirst = false;
+      for (int j = 0; j < bp.k; ++j) bp.lpos[j] = (uint8_t)local[j];
+      bp.term_begin = (uint32_t)vterms.size();
+      for (uint32_t t : take) {
+        const spz_pauli_term& tm = terms[in.term_offset + t];
+        HTerm h{};
+        h.coeff = tm.coeff;
+        h.x_global = tm.x_mask;
+        h.z_mask = tm.z_mask;
+        h.ny = __builtin_popcountll(tm.x_mask & tm.z_mask);
+        for (int q = 0; q < 64; ++q)
+          if ((tm.x_mask >> q) & 1) h.x_local |= 1ull << where[q];
+        vterms.push_back(h);
+        done[t] = 1;
+        remaining--;
+      }
+      bp.term_count = (uint32_t)(vterms.size() - bp.term_begin);
+      vpass.push_back(bp);
+      b->ham_passes++;
+    }
+    // backward: the applied order reversed, as inverse gates with gradients
+    std::vector<GateApp> bwd;
+    for (size_t j = applied.size(); j-- > 0;) {
+      GateApp inv;
+      int rc = make_gate_app(n, inverse_of(fwd_gate[applied[j].src]), applied[j].target, applied[j].ones,
+                             applied[j].zeros, &inv);
+      if (rc) return rc;
+      inv.src = applied[j].src;
+      bwd.push_back(inv);
+    }
+    std::vector<PlannedPass> bp_list;
+    if (I.resident) {
+      if (!bwd.empty()) bp_list.push_back(PlannedPass{all_local, bwd});
+    } else {
+      bp_list = plan_passes(bwd, n, k, c);
+    }
+    for (const PlannedPass& P : bp_list) {
+      // split passes with more gradient slots than the accumulators hold
+      size_t g0 = 0;
+      while (g0 < P.gates.size()) {
+        BPass bp{};
+        bp.kind = BP_BWD;
+        bp.k = (int)P.local.size();
+        bp.c = c;
+        bp.nhigh = bp.k - c;
+        for (int j = 0; j < bp.k; ++j) bp.lpos[j] = (uint8_t)P.local[j];
+        bp.gate_begin = (uint32_t)vgates.size();
+        int slots = 0;
+        size_t g1 = g0;
+        for (; g1 < P.gates.size(); ++g1) {
+          const GateApp& g = P.gates[g1];
+          const int pj = param_of_op[g.src];
+          if (pj >= 0 && slots == kMaxPassParams) break;
+          BGate t = to_bgate(g, P.local);
+          if (pj >= 0) {
+            t.param = pj;
+            t.sign = -1;
+            t.gacc = slots++;
+            switch (g.kind) {
+              case SPZ_GATE_RX: t.grad = BG_X; break;
+              case SPZ_GATE_RY: t.grad = BG_Y; break;
+              case SPZ_GATE_RZ: t.grad = BG_Z; break;
+              default: t.grad = BG_P1; break;
+            }
+            jobs.push_back(CoefJob{(uint32_t)vgates.size(), g.kind, (int64_t)in.param_offset + pj, -1, 0});
+          }
+          vgates.push_back(t);
+        }
+        bp.gate_count = (uint32_t)(vgates.size() - bp.gate_begin);
+        bp.nparams = slots;
+        vpass.push_back(bp);
+        b->bwd_passes++;
+        g0 = g1;
+      }
+    }
+    I.npass = (uint32_t)(vpass.size() - I.pass_begin);
+    b->resident += I.resident;
+    cost[ii] = (double)(applied.size() + 8) * (double)(1ull << n);
+  }
+  std::vector<uint32_t> order(ninst);
+  std::iota(order.begin(), order.end(), 0u);
+  std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t c2) { return cost[a] > cost[c2]; });
+  b->ninst = (uint32_t)ninst;
+  b->nparams_total = ptotal;
+  b->ws_qubits = ws_qubits;
+  b->njobs = (uint32_t)jobs.size();
+  int rc;
+  if ((rc = upload(&b->d_inst, vinst)) || (rc = upload(&b->d_order, order)) || (rc = upload(&b->d_pass, vpass)) ||
+      (rc = upload(&b->d_gates, vgates)) || (rc = upload(&b->d_terms, vterms)) || (rc = upload(&b->d_jobs, jobs)))
+    return rc;
+  SPZ_CUDA(cudaMalloc(&b->d_theta, std::max<uint64_t>(1, ptotal) * sizeof(double)));
+  SPZ_CUDA(cudaMalloc(&b->d_grad, std::max<uint64_t>(1, ptotal) * sizeof(double)));
+  SPZ_CUDA(cudaMalloc(&b->d_energy, std::max<size_t>(1, ninst) * sizeof(double)));
+  SPZ_CUDA(cudaMalloc(&b->d_counter, sizeof(unsigned int)));
+  SPZ_CUDA(cudaMemset(b->d_grad, 0, std::max<uint64_t>(1, ptotal) * sizeof(double)));
+  SPZ_CUDA(cudaMallocHost(&b->h_theta, std::max<uint64_t>(1, ptotal) * sizeof(double)));
+  SPZ_CUDA(cudaMallocHost(&b->h_grad, std::max<uint64_t>(1, ptotal) * sizeof(double)));
+  SPZ_CUDA(cudaMallocHost(&b->h_energy, std::max<size_t>(1, ninst) * sizeof(double)));
+  // launch shape: persistent CTAs, as many per SM as shared memory allows
+  const uint32_t TMAX = 1u << b->kmax;
+  b->smem = (4 * TMAX + (TMAX >> kBatchLowBits) + 64 + kMaxPassParams) * sizeof(double);
+  SPZ_CUDA(cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem));
+  int per_sm = 0;
+  SPZ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel, b->threads, b->smem));
+  if (per_sm < 1) return fail(SPZ_ERR_UNSUPPORTED, "batch kernel does not fit on an SM with this configuration");
+  int sms = 0;
+  SPZ_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device));
+  b->grid = std::max(1, std::min<int>(sms * per_sm, (int)ninst));
+  if (ws_qubits) {
+    // Each CTA owns psi and lam of the largest streamed instance; keep the
+    // workspace within kWorkspaceBudget (at least one CTA per SM).
+    const uint64_t per_cta = 4ull * (1ull << ws_qubits) * sizeof(double);
+    const uint64_t cap = std::max<uint64_t>((uint64_t)sms, kWorkspaceBudget / per_cta);
+    b->grid = (int)std::min<uint64_t>((uint64_t)b->grid, cap);
+    const size_t bytes = (size_t)b->grid * 4 * (1ull << ws_qubits) * sizeof(double);
+    SPZ_CUDA(cudaMalloc(&b->d_ws, bytes));
+  }
+  return SPZ_OK;
+}
+
+int capture_graph(spz_batch_t b) {
+  cudaGraph_t g;
+  SPZ_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+  cudaMemcpyAsync(b->d_theta, b->h_theta, std::max<uint64_t>(1, b->nparams_total) * sizeof(double),
+                  cudaMemcpyHostToDevice, b->stream);
+  cudaMemsetAsync(b->d_counter, 0, sizeof(unsigned int), b->stream);
+  if (b->njobs) batch_coef_kernel<<<(b->njobs + 255) / 256, 256, 0, b->stream>>>(b->d_gates, b->d_jobs, b->njobs, b->d_theta);
+  BatchArgs A{};
+  A.inst = b->d_inst;
+  A.order = b->d_order;
+  A.ninst = b->ninst;
+  A.passes = b->d_pass;
+  A.gates = b->d_gates;
+  A.terms = b->d_terms;
+  A.energies = b->d_energy;
+  A.grads = b->d_grad;
+  A.workspace = b->d_ws;
+  A.ws_qubits = b->ws_qubits;
+  A.counter = b->d_counter;
+  A.kmax = b->kmax;
+  batch_kernel<<<b->grid, b->threads, b->smem, b->stream>>>(A);
+  cudaMemcpyAsync(b->h_energy, b->d_energy, std::max<size_t>(1, b->ninst) * sizeof(double), cudaMemcpyDeviceToHost,
+                  b->stream);
+  cudaMemcpyAsync(b->h_grad, b->d_grad, std::max<uint64_t>(1, b->nparams_total) * sizeof(double),
+                  cudaMemcpyDeviceToHost, b->stream);
+  cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+  if (e != cudaSuccess) return cuda_fail(e, "batch graph capture");
+  e = cudaGraphInstantiate(&b->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return cuda_fail(e, "batch graph instantiation");
+  return SPZ_OK;
+}
+
+}  // namespace
+}  // namespace spz
+
+using namespace spz;
+
+extern "C" {
+
+int spz_batch_create(const spz_batch_instance* instances, size_t ninstances, const spz_op* ops,
+                     const uint32_t* param_index, const spz_pauli_term* terms, const spz_batch_config* config,
+                     spz_batch_t* out) {
+  if (!out || (ninstances && !instances)) return fail(SPZ_ERR_NULL, "NULL argument");
+  spz_batch_t b = new (std::nothrow) spz_batch_s();
+  if (!b) return fail(SPZ_ERR_OUT_OF_MEMORY, "host allocation failed");
+  if (config) {
+    if (config->tile_qubits) b->kmax = config->tile_qubits;
+    if (config->threads) b->threads = config->threads;
+  }
+  if (b->kmax < 4 || b->kmax > kBatchMaxK || b->threads < 64 || b->threads > 1024 || (b->threads & 31)) {
+    delete b;
+    return fail(SPZ_ERR_INVALID_ARGUMENT, "batch config: tile_qubits in 4..12, threads a multiple of 32 in 64..1024");
+  }
+  cudaError_t e = cudaGetDevice(&b->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    delete b;
+    return cuda_fail(e, "batch stream");
+  }
+  int rc = build_batch(b, instances, ninstances, ops, param_index, terms);
+  if (rc) {
+    free_batch(b);
+    return rc;
+  }
+  *out = b;
+  return SPZ_OK;
+}
+
+int spz_batch_run(spz_batch_t b, const double* theta, double* energies, double* grads) {
+  if (!b || !theta || !energies || (b->nparams_total && !grads)) return fail(SPZ_ERR_NULL, "NULL argument");
+  std::memcpy(b->h_theta, theta, b->nparams_total * sizeof(double));
+  if (!b->graph) {
+    int rc = capture_graph(b);
+    if (rc) return rc;
+  }
+  SPZ_CUDA(cudaGraphLaunch(b->graph, b->stream));
+  SPZ_CUDA(cudaStreamSynchronize(b->stream));
+  std::memcpy(energies, b->h_energy, b->ninst * sizeof(double));
+  if (b->nparams_total) std::memcpy(grads, b->h_grad, b->nparams_total * sizeof(double));
+  return SPZ_OK;
+}
+
+int spz_batch_info(spz_batch_t b, spz_batch_stats* st) {
+  if (!b || !st) return fail(SPZ_ERR_NULL, "NULL argument");
+  st->instances = b->ninst;
+  st->resident_instances = b->resident;
+  st->forward_passes = b->fwd_passes;
+  st->hamiltonian_passes = b->ham_passes;
+  st->backward_passes = b->bwd_passes;
+  st->ctas = (uint64_t)b->grid;
+  st->workspace_bytes = b->ws_qubits ? (uint64_t)b->grid * 4 * (1ull << b->ws_qubits) * sizeof(double) : 0;
+  st->tile_qubits = b->kmax;
+  st->threads = b->threads;
+  return SPZ_OK;
+}
+
+int spz_batch_destroy(spz_batch_t b) {
+  if (b) cudaStreamSynchronize(b->stream);
+  free_batch(b);
+  return SPZ_OK;
+}
+
+}  // extern "C"

@@ -201,11 +201,6 @@ inline uint64_t d_mask(const GateApp& g) {
   return m;
 }
 
-struct PlannedPass {
-  std::vector<int> local;        // sorted local qubits
-  std::vector<GateApp> gates;
-};
-
 // Greedy planner: see the file comment.  `k` local qubits per pass, the low
 // `c` qubits always local.
 std::vector<PlannedPass> plan(const std::vector<GateApp>& gates, uint32_t n, int k, int c) {
@@ -315,9 +310,6 @@ TileGate tile_gate(const GateApp& g, const std::vector<int>& local) {
   return t;
 }
 
-struct Segment {
-  std::vector<GateApp> gates;
-};
 
 }  // namespace
 
@@ -365,6 +357,15 @@ struct PassTimer {
 };
 
 }  // namespace
+
+std::vector<PlannedPass> plan_passes(const std::vector<GateApp>& gates, uint32_t n, int k, int c) {
+  return plan(gates, n, k, c);
+}
+
+bool exactly_commuting_kinds(int a, int b) {
+  const int ea = exact_class(a), eb = exact_class(b);
+  return ea == EC_PERM || eb == EC_PERM || (ea == EC_Y && eb != EC_FMA) || (eb == EC_Y && ea != EC_FMA);
+}
 
 // Run a list of already validated gate applications on h.
 int run_gates(spz_state_t h, const std::vector<GateApp>& gates, uint32_t flags, spz_exec_stats* st) {

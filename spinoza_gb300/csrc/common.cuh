@@ -136,6 +136,14 @@ uint64_t gate_algorithmic_bytes(uint32_t n, const GateApp& g);
 // application needs on 2^n amplitudes.
 uint64_t gate_fp64_ops(uint32_t n, const GateApp& g);
 
+// Fusion planner (circuit.cu): passes of gates over tiles of k local qubits,
+// the low c qubits always local.
+struct PlannedPass {
+  std::vector<int> local;  // sorted local qubits
+  std::vector<GateApp> gates;
+};
+std::vector<PlannedPass> plan_passes(const std::vector<GateApp>& gates, uint32_t n, int k, int c);
+
 // Reductions used by measurement and the executor.
 int prob0_device(spz_state_t h, uint32_t target, double* out);
 int collapse_device(spz_state_t h, uint32_t target, int outcome, double scale);

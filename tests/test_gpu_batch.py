@@ -1,0 +1,87 @@
+"""The batched forward + adjoint launch vs the single-instance adjoint path and
+the oracle.  Small tiles (tile_qubits=4..6) force the streaming (non-resident)
+path, multiple Hamiltonian passes and split backward passes at small sizes."""
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+from spinoza_gb300 import adjoint, batch
+from spinoza_gb300.core import State
+
+pytestmark = pytest.mark.gpu
+
+
+def _single(inst):
+    n, ops, pidx, theta, terms = inst
+    return adjoint.adjoint_gradient(State(n), adjoint.set_params(ops, pidx, theta), pidx, terms)
+
+
+def _instances():
+    shapes = [(3, 1), (5, 2), (8, 3), (2, 2), (13, 2), (14, 1), (9, 4), (1, 2), (11, 1), (6, 3)]
+    return [batch.hea_instance(n, d, 100 + i) for i, (n, d) in enumerate(shapes)]
+
+
+@pytest.mark.parametrize("tile_qubits,threads", [(12, 512), (4, 64), (5, 128), (6, 1024)])
+def test_batch_matches_single_instance_adjoint(gpu, tile_qubits, threads):
+    insts = _instances()
+    b = batch.Batch(insts, tile_qubits=tile_qubits, threads=threads)
+    e, g = b.run()
+    for i, inst in enumerate(insts):
+        e1, g1 = _single(inst)
+        assert abs(e[i] - e1) < 1e-12 * max(1.0, abs(e1)), (i, e[i], e1)
+        np.testing.assert_allclose(b.split(g)[i], g1, atol=1e-11, rtol=0)
+    info = b.info()
+    assert info["instances"] == len(insts)
+    if tile_qubits == 4:
+        assert info["resident_instances"] < len(insts) and info["workspace_bytes"] > 0
+
+
+def test_batch_graph_replay_with_new_angles(gpu):
+    insts = _instances()[:5]
+    b = batch.Batch(insts, tile_qubits=5, threads=128)
+    b.run()
+    theta2 = b.theta + 0.37
+    e, g = b.run(theta2)
+    for i, (n, ops, pidx, _, terms) in enumerate(insts):
+        th = b.split(theta2)[i]
+        e1, g1 = adjoint.adjoint_gradient(State(n), adjoint.set_params(ops, pidx, th), pidx, terms)
+        assert abs(e[i] - e1) < 1e-12 * max(1.0, abs(e1))
+        np.testing.assert_allclose(b.split(g)[i], g1, atol=1e-11, rtol=0)
+
+
+def test_batch_gradient_matches_oracle_parameter_shift(gpu):
+    n, ops, pidx, theta, terms = batch.hea_instance(4, 2, 7)
+    b = batch.Batch([(n, ops, pidx, theta, terms)], tile_qubits=4, threads=64)
+    _, g = b.run()
+
+    def energy(th):
+        re, im = oracle.zero_state(n)
+        oracle.execute(adjoint.set_params(ops, pidx, th), re, im)
+        return oracle.pauli_expectation(re, im, terms)
+
+    for j in range(len(pidx)):
+        tp, tm = theta.copy(), theta.copy()
+        tp[j] += math.pi / 2
+        tm[j] -= math.pi / 2
+        assert abs(g[j] - 0.5 * (energy(tp) - energy(tm))) < 1e-9
+
+
+def test_batch_rejects_bad_input(gpu):
+    n, ops, pidx, theta, terms = batch.hea_instance(3, 1, 1)
+    with pytest.raises(ValueError):
+        batch.Batch([(n, ops, pidx, theta, terms)], tile_qubits=13)
+    bad = pidx.copy()
+    bad[0] = len(ops) + 5
+    with pytest.raises(ValueError):
+        batch.Batch([(n, ops, bad, theta, terms)])
+
+
+def test_config5_generator_shapes():
+    insts = batch.config5_instances(count=64)
+    qs = [i[0] for i in insts]
+    assert min(qs) >= 10 and max(qs) <= 22
+    for n, ops, pidx, theta, terms in insts:
+        assert len(pidx) % (2 * n) == 0 and 2 <= len(pidx) // (2 * n) <= 10
+        assert len(terms) == 2 * n - 1
