@@ -254,12 +254,17 @@ def gpu_arm(args) -> None:
     n, layers = args.qubits, args.layers
     ops = brickwork_ops(n, layers)
     abytes = algorithmic_bytes(ops, n)
-    state = State(n)
+    N = 1 << n
+    mode = nat.EXEC_DEFAULT if args.exact else nat.EXEC_FAST
+    re_t = torch.empty(N, dtype=torch.float64, device="cuda")
+    im_t = torch.empty(N, dtype=torch.float64, device="cuda")
+    state = State.from_torch(re_t, im_t)
     stream = torch.cuda.current_stream()
-    nat.check(nat.lib().spz_state_set_stream(state.handle, nat.c_void_p(stream.cuda_stream)))
-    qc = QuantumCircuit.from_state(state)
+    state.set_stream(stream)  # events on torch's stream bracket the kernels
+    qc = QuantumCircuit.from_state(state, fast=not args.exact)
 
-    def step(flags=nat.EXEC_DEFAULT):
+    def step(flags=0):
+        flags |= mode
         state.reset_zero()
         st = nat.spz_exec_stats()
         nat.check(nat.lib().spz_circuit_execute(state.handle, nat.ptr(ops), len(ops), nat.byref(qc.qubit_tracker.c),
@@ -315,7 +320,7 @@ def gpu_arm(args) -> None:
             nat.check(nat.lib().spz_state_upload(state.handle, nat.c_void_p(hin_re.data_ptr()),
                                                  nat.c_void_p(hin_im.data_ptr())))
             nat.check(nat.lib().spz_circuit_execute(state.handle, nat.ptr(ops), len(ops),
-                                                    nat.byref(qc.qubit_tracker.c), nat.EXEC_DEFAULT, None))
+                                                    nat.byref(qc.qubit_tracker.c), mode, None))
             nat.check(nat.lib().spz_state_download(state.handle, nat.c_void_p(hout_re.data_ptr()),
                                                    nat.c_void_p(hout_im.data_ptr())))
 
@@ -331,6 +336,30 @@ def gpu_arm(args) -> None:
                "api": "spz_state_upload + spz_circuit_execute + spz_state_download (pinned host buffers)"}
         del hin_re, hin_im, hout_re, hout_im
 
+    # Parity at full size: the exact (reference-arithmetic, bit-identical to the
+    # oracle's sequence) mode on a second state; max |difference| of the amplitudes.
+    parity = None
+    if not args.exact and not args.no_parity:
+        re2 = torch.empty(N, dtype=torch.float64, device="cuda")
+        im2 = torch.empty(N, dtype=torch.float64, device="cuda")
+        s2 = State.from_torch(re2, im2)
+        s2.reset_zero()
+        q2 = QuantumCircuit.from_state(s2)
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        t0.record()
+        q2.execute_ops(ops)
+        t1.record()
+        torch.cuda.synchronize()
+        state.reset_zero()
+        qc.execute_ops(ops)  # a fresh fast run to compare against
+        torch.cuda.synchronize()
+        d = max(float((re_t - re2).abs().max()), float((im_t - im2).abs().max()))
+        parity = {"max_abs_diff_fast_vs_exact": d, "bound": 1e-12, "ok": d <= 1e-12,
+                  "exact_ms_per_step": t0.elapsed_time(t1),
+                  "exact_gbs": abytes / (t0.elapsed_time(t1) / 1e3) / 1e9,
+                  "max_abs_amplitude": max(float(re_t.abs().max()), float(im_t.abs().max()))}
+        del s2, q2, re2, im2
     adj = None if args.no_adjoint or rank != 0 else adjoint_bench()
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -349,7 +378,9 @@ def gpu_arm(args) -> None:
                                    f"U[0,2pi) seed 2, + CX even/odd ladders; from |0...0>)",
                        "qubits": n, "layers": layers, "gates": int(len(ops)), "state_bytes": 16 * N,
                        "l2": "inputs larger than L2 (16 GiB state vs 129 MB L2); no flush",
-                       "executor": "fused shared-memory tile passes, exact reference arithmetic",
+                       "executor": ("fused shared-memory tile passes, exact reference arithmetic" if args.exact else
+                                    "fused shared-memory tile passes, fast arithmetic (lazy scaling, U = P RY P, "
+                                    "phases pushed through permutations); equal to exact up to rounding"),
                        "parallelism": "replicas" if world > 1 else "single-gpu"},
             "gates_per_s": len(ops) * world * args.steps / (ms / 1e3),
             "passes_per_step": int(launches / args.steps) - 1,
@@ -363,6 +394,7 @@ def gpu_arm(args) -> None:
                      "note": "FP64-pipe instructions the gates need / device time of the passes; peak = DFMA issue "
                              "rate measured live on this GPU before and after the timed region "
                              "(spz_probe_fp64_fma_rate), the larger of the two"},
+            "parity": parity,
             "cpu_baseline": cpu,
             "e2e": e2e,
             "gpu_launches": int(launches),
@@ -374,22 +406,205 @@ def gpu_arm(args) -> None:
         dist.destroy_process_group()
 
 
+# ------------------------------------------------------------ other configs
+def _line(metric: str, value: float, unit: str, args, **extra) -> None:
+    d = {"metric": metric, "value": value, "unit": unit, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+         "dtype": "f64", "data": "synthetic"}
+    d.update(extra)
+    print(json.dumps(d), flush=True)
+
+
+def _event_time(fn, steps: int, warmup: int) -> float:
+    """Mean seconds per call, CUDA events on torch's current stream, synchronised around."""
+    import torch
+
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / 1e3 / steps
+
+
+def workload_qft20(args) -> None:
+    """Config 1: QFT with swaps on a seeded N(0,1) normalised 20-qubit state."""
+    import oracle
+    from spinoza_gb300 import _native as nat
+    from spinoza_gb300 import circuit, rng
+    from spinoza_gb300.circuit import QuantumCircuit
+    from spinoza_gb300.core import State
+
+    n = 20
+    qc = QuantumCircuit.__new__(QuantumCircuit)
+    qc.transformations = []
+    for j in range(n - 1, -1, -1):
+        qc.h(j)
+        for k in range(j - 1, -1, -1):
+            qc.cp(math.pi / 2 ** (j - k), j, k)
+    for i in range(n // 2):
+        qc.swap(i, n - 1 - i)
+    ops = circuit._ops_array(qc.transformations, lambda: 0.0)
+    import torch
+
+    init = rng.normal_state(n, 1)
+    src, s = State.from_arrays(*init), State(n)
+    src.set_stream(torch.cuda.current_stream())
+    s.set_stream(torch.cuda.current_stream())
+    runner = QuantumCircuit.from_state(s)
+    out = {}
+    for name, fused in (("fused", True), ("unfused", False)):
+        runner.fused = fused
+
+        def step():
+            nat.check(nat.lib().spz_state_copy(s.handle, src.handle))
+            runner.execute_ops(ops)
+
+        out[name] = _event_time(step, args.steps * 20, args.warmup)
+    re, im = init[0].copy(), init[1].copy()
+    t0 = time.perf_counter()
+    oracle.execute(ops, re, im)
+    t_cpu = time.perf_counter() - t0
+    gre, gim = s.to_numpy()
+    d = float(max(np.max(np.abs(gre - re)), np.max(np.abs(gim - im))))
+    abytes = algorithmic_bytes(ops, n)
+    _line("config1 QFT-20 circuit time", out["fused"] * 1e3, "ms", args, higher_is_better=False,
+          config={"workload": "QFT with swaps, 20 qubits, N(0,1) normalised state seed 1", "gates": len(ops)},
+          unfused_ms=out["unfused"] * 1e3, effective_gbs=abytes / out["fused"] / 1e9,
+          passes=circuit.plan_stats(n, ops)["passes"], cpu_baseline_ms=t_cpu * 1e3, cpu_threads=oracle.num_threads(),
+          max_abs_diff_vs_oracle=d, bit_identical=bool(d == 0.0))
+
+
+def workload_measure28(args) -> None:
+    """Config 3: 28 qubits, 1e6 seeded shots (bit-exact rule) and <H> = sum a ZZ + b X."""
+    from spinoza_gb300 import core, rng
+    from spinoza_gb300.core import State
+
+    n = 28
+    s = State(n)
+    s.fill_random(3, "normal", normalise=True)
+    u = rng.uniforms(4, 1_000_000)
+    t_shots = _event_time(lambda: core.sample(s, u), args.steps, 1)
+    ab = rng.uniforms(5, 4 * n)
+    a = np.sqrt(-2 * np.log1p(-ab[:n - 1])) * np.cos(2 * math.pi * ab[n:2 * n - 1])
+    b = np.sqrt(-2 * np.log1p(-ab[2 * n:3 * n])) * np.cos(2 * math.pi * ab[3 * n:4 * n])
+    H = core.ising_hamiltonian(a, b)
+    t_h = _event_time(lambda: core.pauli_expectation(s, H), args.steps, 1)
+    N = 1 << n
+    _line("config3 shots/s at 28 qubits", 1e6 / t_shots, "shots/s", args, higher_is_better=True,
+          config={"workload": "28-qubit N(0,1) normalised state, 1e6 shots (uniform seed 4), <H> with "
+                              "a_i, b_i ~ N(0,1) (seed 5)", "terms": int(len(H))},
+          sample_ms=t_shots * 1e3, sample_gbs=(24 * N) / t_shots / 1e9, expectation_ms=t_h * 1e3,
+          expectation_gbs=(16 * N) / t_h / 1e9, energy=core.pauli_expectation(s, H))
+
+
+def workload_batch(args) -> None:
+    """Config 5: 4096 instances, qubits 10..22, depth 2..10; one persistent launch vs a loop."""
+    from spinoza_gb300 import adjoint, batch
+    from spinoza_gb300.core import State
+
+    t0 = time.perf_counter()
+    insts = batch.config5_instances(args.instances)
+    t_build = time.perf_counter() - t0
+    tune = batch.autotune(insts, reps=1) if args.autotune else {"tile_qubits": 12, "threads": 512}
+    b = batch.Batch(insts, tile_qubits=tune["tile_qubits"], threads=tune["threads"])
+    b.run()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e, g = b.run()
+    t_batch = (time.perf_counter() - t0) / args.steps
+    # baseline: the per-instance path (spz_adjoint_gradient) on a stratified sample
+    order = sorted(range(len(insts)), key=lambda i: insts[i][0] * 1000 + len(insts[i][1]))
+    sample = order[:: max(1, len(order) // args.loop_sample)]
+    t_loop_sample = 0.0
+    max_e, max_g = 0.0, 0.0
+    for i in sample:
+        n, ops, pidx, theta, terms = insts[i]
+        t1 = time.perf_counter()
+        e1, g1 = adjoint.adjoint_gradient(State(n), adjoint.set_params(ops, pidx, theta), pidx, terms)
+        t_loop_sample += time.perf_counter() - t1
+        max_e = max(max_e, abs(e1 - e[i]))
+        max_g = max(max_g, float(np.max(np.abs(g1 - b.split(g)[i]))))
+    t_loop = t_loop_sample * len(insts) / len(sample)
+    nparams = int(b.theta.size)
+    _line("config5 batched forward+adjoint instances/s", len(insts) / t_batch, "instances/s", args,
+          higher_is_better=True,
+          config={"workload": f"{len(insts)} HEA instances (RY/RZ layers + CZ ring), qubits U{{10..22}}, depth "
+                              f"U{{2..10}}, seeds 8+k", "params": nparams, "launch": tune},
+          seconds_per_batch=t_batch, grads_per_s=nparams / t_batch, loop_seconds_extrapolated=t_loop,
+          loop_sample=len(sample), speedup_vs_loop=t_loop / t_batch, max_abs_energy_diff=max_e,
+          max_abs_grad_diff=max_g, build_seconds=t_build, info=b.info())
+
+
+def workload_sweep33(args) -> None:
+    """Config 2 sweep: H, RZ, CX and 3-control X on every target at 33 qubits (128 GiB)."""
+    import torch
+
+    from spinoza_gb300 import gates as G
+    from spinoza_gb300.core import State
+    from spinoza_gb300.gates import Gate
+
+    n = args.qubits if args.qubits != 30 else 33
+    N = 1 << n
+    re = torch.empty(N, dtype=torch.float64, device="cuda")
+    im = torch.empty(N, dtype=torch.float64, device="cuda")
+    s = State.from_torch(re, im)
+    s.fill_random(11, "uniform", normalise=False)
+    peaks = measured_peaks()
+    rows = []
+    kinds = [("H", lambda t: G.apply(Gate.H, s, t), 32),
+             ("RZ", lambda t: G.apply(Gate.RZ(0.7), s, t), 32),
+             ("CX", lambda t: G.c_apply(Gate.X, s, (t + 1) % n, t), 16),
+             ("MCX3", lambda t: G.mc_apply(Gate.X, s, [(t + 1) % n, (t + 2) % n, (t + 3) % n], None, t), 4)]
+    for name, fn, bpn in kinds:
+        for t in range(n):
+            dt = _event_time(lambda: fn(t), 1, 1)
+            gbs = bpn * N / dt / 1e9
+            rows.append({"gate": name, "target": t, "ms": dt * 1e3, "gbs": gbs, "frac": gbs / peaks["hbm_gbs"]})
+    summary = {}
+    for name, _, _ in kinds:
+        r = [x for x in rows if x["gate"] == name]
+        summary[name] = {"ms_median": statistics.median(x["ms"] for x in r),
+                         "gbs_median": statistics.median(x["gbs"] for x in r),
+                         "frac_median": statistics.median(x["frac"] for x in r),
+                         "frac_min": min(x["frac"] for x in r)}
+    _line(f"config2 per-gate sweep at {n} qubits", summary["H"]["gbs_median"], "GB/s", args, higher_is_better=True,
+          config={"workload": f"H, RZ(0.7), CX(control (t+1) mod n), X with 3 controls (t+1..t+3 mod n), "
+                              f"targets 0..{n - 1}, {n} qubits ({16 * N >> 30} GiB)"},
+          summary=summary, rows=rows, peak_gbs=peaks["hbm_gbs"])
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="brickwork", choices=["brickwork", "qft20", "measure28", "batch", "sweep33"])
     ap.add_argument("--qubits", type=int, default=30)
     ap.add_argument("--layers", type=int, default=20)
+    ap.add_argument("--instances", type=int, default=4096)
+    ap.add_argument("--loop-sample", type=int, default=64)
+    ap.add_argument("--autotune", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-parity", action="store_true")
+    ap.add_argument("--exact", action="store_true", help="time the bit-exact executor mode instead of fast mode")
     args = ap.parse_args()
     if args.impl == "reference":
         reference_arm(args)
-    else:
+    elif args.workload == "brickwork":
         gpu_arm(args)
+    else:
+        import torch
+
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        {"qft20": workload_qft20, "measure28": workload_measure28, "batch": workload_batch,
+         "sweep33": workload_sweep33}[args.workload](args)
 
 
 if __name__ == "__main__":

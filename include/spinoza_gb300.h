@@ -92,7 +92,7 @@ int spz_state_wrap(uint32_t n, double* d_reals, double* d_imags, spz_state_t* ou
 int spz_state_destroy(spz_state_t h);
 
 /* Issue all later work of this handle on `stream` (a cudaStream_t; NULL = the
- * handle's own stream). */
+ * handle's own stream; pass cudaStreamLegacy for the legacy default stream). */
 int spz_state_set_stream(spz_state_t h, void* stream);
 
 /* Wait until all work issued on the handle's stream has finished. */
@@ -145,6 +145,15 @@ int spz_cc_apply(spz_state_t h, const spz_gate* gate, uint32_t control0, uint32_
 int spz_mc_apply(spz_state_t h, const spz_gate* gate, const uint32_t* controls,
                  uint32_t ncontrols, const uint32_t* zeros, uint32_t nzeros, uint32_t target);
 
+/* transform_u / c_transform_u (spinoza/src/gates.rs:1427-1487) and
+ * unitaries::apply_unitary (spinoza/src/unitaries.rs): apply a 2^m x 2^m complex
+ * matrix (row-major, separate real and imaginary arrays, like `Unitary`) to
+ * qubits target .. target+m-1 (bit target+j of an index is bit j of the row /
+ * column), only where `control` reads 1 when control >= 0.  m in 1..12; the
+ * control must lie outside the block.  Uses one state-sized work vector. */
+int spz_apply_unitary(spz_state_t h, const double* u_reals, const double* u_imags, uint32_t m,
+                      uint32_t target, int32_t control);
+
 /* ---------------------------------------------------------------- circuits */
 /* Control kinds of a transformation; same variants as `enum Controls`
  * (spinoza/src/circuit.rs:55-69). */
@@ -175,6 +184,9 @@ typedef struct spz_tracker {
 #define SPZ_EXEC_DEFAULT 0u      /* fused executor: runs of gates per shared-memory tile  */
 #define SPZ_EXEC_UNFUSED 1u      /* one kernel per gate (the plain per-gate path)         */
 #define SPZ_EXEC_TIME_PASSES 4u  /* time every pass with CUDA events (synchronises once)  */
+#define SPZ_EXEC_FAST 8u         /* fused, with arithmetic rewritten to need fewer FP64
+                                    instructions (lazy scaling, phase pushing); equal to
+                                    the exact mode up to rounding, not bit-identical     */
 
 /* Execution counters filled by spz_circuit_execute (may be NULL). */
 typedef struct spz_exec_stats {

@@ -49,6 +49,7 @@ def lib():
             "orc_pauli_expectation": [c_int, v, v, v, c_uint64, POINTER(d)],
             "orc_iqft": [c_int, v, v, v, c_uint32],
             "orc_sample": [c_int, v, v, v, c_uint64, v],
+            "orc_apply_unitary": [c_int, v, v, v, v, c_int, c_int, c_int],
             "orc_stream_u64": [c_uint64, c_uint64],
             "orc_stream_uniform": [c_uint64, c_uint64],
             "orc_fill_uniform": [c_int, v, v, c_uint64],
@@ -161,6 +162,13 @@ def pauli_expectation(re, im, terms: np.ndarray) -> float:
 def iqft(re, im, targets: Sequence[int]) -> None:
     t = np.ascontiguousarray(np.array(targets, dtype=np.uint32))
     _check(lib().orc_iqft(_n(re), _p(re), _p(im), _p(t), len(t)))
+
+
+def apply_unitary(re, im, matrix: np.ndarray, target: int, control: int = -1) -> None:
+    mr = np.ascontiguousarray(matrix.real, dtype=np.float64)
+    mi = np.ascontiguousarray(matrix.imag, dtype=np.float64)
+    m = int(matrix.shape[0]).bit_length() - 1
+    _check(lib().orc_apply_unitary(_n(re), _p(re), _p(im), _p(mr), _p(mi), m, target, control))
 
 
 def sample(re, im, u: np.ndarray) -> np.ndarray:

@@ -554,6 +554,37 @@ int orc_iqft(int n, double* re, double* im, const uint32_t* targets, uint32_t nt
   return OK;
 }
 
+// transform_u / c_transform_u (gates.rs:1427-1487) with the state's own n
+// (the reference takes n from the matrix width, gates.rs:1430) and the
+// row accumulation of unitary_col_vec_mul (gates.rs:1388-1425):
+// re += a*v_re - b*v_im; im += a*v_im + b*v_re, j ascending.
+int orc_apply_unitary(int n, double* re, double* im, const double* ur, const double* ui, int m, int t, int control) {
+  if (m < 1 || t < 0 || t + m > n) return EINVAL_;
+  if (control >= 0 && (control >= n || (control >= t && control < t + m))) return EINVAL_;
+  const uint64_t N = 1ull << n, M = 1ull << m;
+  std::vector<double> vr(M), vi(M);
+  for (uint64_t suffix = 0; suffix < (1ull << t); ++suffix)
+    for (uint64_t prefix = 0; prefix < (N >> (t + m)); ++prefix) {
+      const uint64_t base = prefix * (1ull << (t + m)) + suffix;
+      if (control >= 0 && !((base >> control) & 1)) continue;
+      for (uint64_t j = 0; j < M; ++j) {
+        vr[j] = re[base + j * (1ull << t)];
+        vi[j] = im[base + j * (1ull << t)];
+      }
+      for (uint64_t i = 0; i < M; ++i) {
+        double dr = 0.0, di = 0.0;
+        for (uint64_t j = 0; j < M; ++j) {
+          const double a = ur[i * M + j], b = ui[i * M + j];
+          dr += a * vr[j] - b * vi[j];
+          di += a * vi[j] + b * vr[j];
+        }
+        re[base + i * (1ull << t)] = dr;
+        im[base + i * (1ull << t)] = di;
+      }
+    }
+  return OK;
+}
+
 int orc_sample(int n, const double* re, const double* im, const double* u, uint64_t nshots, uint64_t* out) {
   return sample(n, re, im, u, nshots, out);
 }

@@ -30,9 +30,12 @@ H, M, X, Y, Z, P, RX, RY, RZ, SWAP, U, UNITARY, BITFLIP = range(13)
 # enum spz_controls_kind (circuit.rs:55-69)
 CONTROLS_NONE, CONTROLS_SINGLE, CONTROLS_ONES, CONTROLS_MIXED = range(4)
 
+CUDA_STREAM_LEGACY = 0x1  # cudaStreamLegacy: the legacy default stream (torch's stream handle 0)
+
 EXEC_DEFAULT = 0
 EXEC_UNFUSED = 1
 EXEC_TIME_PASSES = 4
+EXEC_FAST = 8
 MAX_QUBITS = 34
 
 
@@ -124,6 +127,7 @@ SIGNATURES = [
     ("spz_c_apply", c_int, [c_void_p, POINTER(spz_gate), c_uint32, c_uint32]),
     ("spz_cc_apply", c_int, [c_void_p, POINTER(spz_gate), c_uint32, c_uint32, c_uint32]),
     ("spz_mc_apply", c_int, [c_void_p, POINTER(spz_gate), c_void_p, c_uint32, c_void_p, c_uint32, c_uint32]),
+    ("spz_apply_unitary", c_int, [c_void_p, c_void_p, c_void_p, c_uint32, c_uint32, c_int32]),
     ("spz_circuit_execute", c_int, [c_void_p, c_void_p, c_size_t, POINTER(spz_tracker), c_uint32,
                                     POINTER(spz_exec_stats)]),
     ("spz_plan_stats", c_int, [c_uint32, c_void_p, c_size_t, c_uint32, POINTER(spz_exec_stats)]),

@@ -125,7 +125,8 @@ def _ops_array(transformations: Sequence[QuantumTransformation], draws) -> np.nd
     for i, tr in enumerate(transformations):
         g = tr.gate
         if g.kind == nat.UNITARY:
-            raise nat.Unsupported(nat.SPZ_ERR_UNSUPPORTED, "dense Unitary transformations are not on this path")
+            raise nat.Unsupported(nat.SPZ_ERR_UNSUPPORTED, "a dense Unitary is not an op; QuantumCircuit.execute "
+                                                          "applies it between op runs")
         p = list(g.params)
         if g.kind == nat.M:
             p[0] = draws()
@@ -148,7 +149,8 @@ class QuantumCircuit:
     measurement outcomes inside execute(); ``fused=False`` runs one kernel per
     gate (the plain per-gate path)."""
 
-    def __init__(self, *registers: QuantumRegister, seed: int = 0, fused: bool = True, state: Optional[State] = None):
+    def __init__(self, *registers: QuantumRegister, seed: int = 0, fused: bool = True, fast: bool = False,
+                 state: Optional[State] = None):
         bits = 0
         sizes = []
         for r in registers:  # circuit.rs:181-198
@@ -157,9 +159,11 @@ class QuantumCircuit:
             bits += len(r)
         self.transformations: List[QuantumTransformation] = []
         self.quantum_registers_info = sizes
-        self.state = state if state is not None else State(bits)
+        self.num_qubits = state.n if state is not None else bits
+        self._state = state  # allocated on the device on first use
         self.qubit_tracker = QubitTracker()
         self.fused = fused
+        self.fast = fast
         self.last_stats = nat.spz_exec_stats()
         self._seed = int(seed)
         self._draw_index = 0
@@ -168,6 +172,17 @@ class QuantumCircuit:
     def from_state(cls, state: State, **kw) -> "QuantumCircuit":
         qc = cls(state=state, **kw)
         return qc
+
+    @property
+    def state(self) -> State:
+        if self._state is None:
+            self._state = State(self.num_qubits)
+        return self._state
+
+    @state.setter
+    def state(self, s: State) -> None:
+        self._state = s
+        self.num_qubits = s.n
 
     def get_statevector(self) -> State:
         return self.state
@@ -255,15 +270,53 @@ class QuantumCircuit:
         return _ops_array(self.transformations, self._next_draw)
 
     def execute(self) -> None:  # circuit.rs:552-600 (drains the transformations)
-        ops = self.ops()
+        trs = self.transformations
         self.transformations = []
-        self.execute_ops(ops)
+        start = 0
+        for i, tr in enumerate(trs + [None]):
+            if tr is not None and tr.gate.kind != nat.UNITARY:
+                continue
+            if i > start:
+                self.execute_ops(_ops_array(trs[start:i], self._next_draw))
+            if tr is not None:  # circuit.rs:555-558: transform_u / c_transform_u
+                from .unitaries import c_transform_u, transform_u
+
+                if tr.controls.kind == Controls.NONE:
+                    transform_u(self.state, tr.gate.matrix, tr.target)
+                elif tr.controls.kind == Controls.SINGLE:
+                    c_transform_u(self.state, tr.gate.matrix, tr.controls.controls[0], tr.target)
+                else:
+                    raise nat.Unsupported(nat.SPZ_ERR_UNSUPPORTED, "a Unitary takes at most one control")
+            start = i + 1
+
+    # dense unitaries (circuit.rs:514-545)
+    def unitary(self, u, target: int) -> None:
+        self._add(Gate.Unitary(u), target)
+
+    def append_u(self, u, qr: QuantumRegister) -> None:
+        if u.height != u.width or u.height != 1 << len(qr):
+            raise nat.InvalidArgument(nat.SPZ_ERR_INVALID_ARGUMENT, "unitary size must be 2^len(register)")
+        self.unitary(u, qr.get_shift())
+
+    def c_unitary(self, u, c: int, t: int) -> None:
+        self._add(Gate.Unitary(u), t, Controls.single(c))
+
+    def c_append_u(self, u, c: int, qr: QuantumRegister) -> None:
+        if u.height != u.width or u.height != 1 << len(qr):
+            raise nat.InvalidArgument(nat.SPZ_ERR_INVALID_ARGUMENT, "unitary size must be 2^len(register)")
+        self.c_unitary(u, c, qr.get_shift())
 
     def execute_ops(self, ops: np.ndarray) -> None:
         ops = np.ascontiguousarray(ops, dtype=nat.OP_DTYPE)
-        flags = nat.EXEC_DEFAULT if self.fused else nat.EXEC_UNFUSED
+        flags = _flags(self.fused, self.fast)
         nat.check(nat.lib().spz_circuit_execute(self.state.handle, nat.ptr(ops), len(ops),
                                                 byref(self.qubit_tracker.c), flags, byref(self.last_stats)))
+
+
+def _flags(fused: bool, fast: bool) -> int:
+    if fast:
+        return nat.EXEC_FAST
+    return nat.EXEC_DEFAULT if fused else nat.EXEC_UNFUSED
 
 
 def plan_schedule(n: int, ops: np.ndarray, fused: bool = True) -> tuple[np.ndarray, np.ndarray]:
@@ -280,10 +333,10 @@ def plan_schedule(n: int, ops: np.ndarray, fused: bool = True) -> tuple[np.ndarr
     return order[: count.value], passes[: count.value]
 
 
-def plan_stats(n: int, ops: np.ndarray, fused: bool = True) -> dict:
+def plan_stats(n: int, ops: np.ndarray, fused: bool = True, fast: bool = False) -> dict:
     """How the executor would fuse `ops` on n qubits (host only, no GPU)."""
     st = nat.spz_exec_stats()
     ops = np.ascontiguousarray(ops, dtype=nat.OP_DTYPE)
-    flags = nat.EXEC_DEFAULT if fused else nat.EXEC_UNFUSED
+    flags = _flags(fused, fast)
     nat.check(nat.lib().spz_plan_stats(int(n), nat.ptr(ops), len(ops), flags, byref(st)))
     return {f: getattr(st, f) for f, _ in nat.spz_exec_stats._fields_}

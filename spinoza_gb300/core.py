@@ -64,8 +64,9 @@ class State:
         n = int(reals.numel()).bit_length() - 1
         h = c_void_p()
         nat.check(nat.lib().spz_state_wrap(n, c_void_p(reals.data_ptr()), c_void_p(imags.data_ptr()), byref(h)))
-        nat.check(nat.lib().spz_state_set_stream(h, c_void_p(torch.cuda.current_stream().cuda_stream)))
-        return cls(n, _handle=h, _keep=(reals, imags))
+        s = cls(n, _handle=h, _keep=(reals, imags))
+        s.set_stream(torch.cuda.current_stream())
+        return s
 
     def __del__(self):
         h = getattr(self, "_h", None)
@@ -126,6 +127,16 @@ class State:
 
     def synchronize(self) -> None:
         nat.check(nat.lib().spz_state_synchronize(self._h))
+
+    def set_stream(self, stream) -> None:
+        """Issue this state's work on `stream`: a torch.cuda.Stream, a raw
+        cudaStream_t as int, or None for the handle's own stream.  torch's
+        default stream (handle 0) maps to cudaStreamLegacy."""
+        if stream is None:
+            nat.check(nat.lib().spz_state_set_stream(self._h, None))
+            return
+        raw = int(getattr(stream, "cuda_stream", stream))
+        nat.check(nat.lib().spz_state_set_stream(self._h, c_void_p(raw if raw else nat.CUDA_STREAM_LEGACY)))
 
     def device_arrays(self) -> tuple[int, int]:
         r, i = c_void_p(), c_void_p()

@@ -29,9 +29,15 @@ int apply_controlled(spz_state_t h, const spz_gate* gate, uint32_t target, uint6
 
 constexpr int kTileMaxK = 12;     // 2^12 amplitudes x 16 B = 64 KiB of shared memory
 constexpr int kTileLowBits = 3;   // qubits 0..2 always local: 64-byte contiguous rows
-constexpr int kTileThreads = 512;
+#ifndef SPZ_TILE_THREADS
+#define SPZ_TILE_THREADS 384  // 3 blocks x 12 warps per SM; 55 registers without spills
+#endif
+#ifndef SPZ_TILE_MIN_BLOCKS
+#define SPZ_TILE_MIN_BLOCKS 3  // 3 x (64 KiB tile + 4 KiB row table) fit one SM's shared memory
+#endif
+constexpr int kTileThreads = SPZ_TILE_THREADS;
 
-enum TileMode { TM_PAIR = 0, TM_DIAG_LOCAL = 1, TM_DIAG_GLOBAL = 2, TM_SWAP = 3 };
+enum TileMode { TM_PAIR = 0, TM_DIAG_LOCAL = 1, TM_DIAG_GLOBAL = 2, TM_SWAP = 3, TM_PHASE = 4 };
 
 struct TileGate {
   int32_t kind;
@@ -45,6 +51,13 @@ struct TileGate {
   uint64_t g_zeros; // non-local bits the tile base must have clear
   uint64_t g_tbit;  // TM_DIAG_GLOBAL: the non-local target bit
   Coef c;
+  // TM_PHASE: amplitude x (with x & half_bit, if half_bit != 0) is multiplied by
+  // table[sum_j parity(x & pmask[j]) << j] (complex, ptab .. ptab + 2^pm - 1).
+  uint64_t half_bit;
+  uint64_t pmask[kPhaseMaxTerms];  // parity masks over the global index
+  uint32_t pemask[kPhaseMaxTerms]; // their local part, as bits of the tile offset e
+  int32_t pm;
+  uint32_t ptab;
 };
 
 struct PassArgs {
@@ -52,6 +65,7 @@ struct PassArgs {
   double* im;
   uint64_t ntiles;
   const TileGate* gates;
+  const double2* tables;  // fast-mode phase tables (re, im)
   int ngates;
   int k;            // local qubits
   int c;            // low contiguous local qubits (0..c-1)
@@ -60,29 +74,156 @@ struct PassArgs {
 };
 
 // ------------------------------------------------------------ device side
-template <int KIND>
+// Every tile op reads its descriptor once, into registers, before its loop:
+// the loop body then touches only shared memory (and, for phase ops, the
+// phase table through L1).
+
+// m -> tile offset with zero bits inserted at the op's sorted local positions
+// (NPOS of them; -1 = any number, read from the descriptor), then l_ones set.
+// Inserting a zero at p is e + (e & ~(2^p - 1)); ascending order keeps the
+// lower insertions in place.
+template <int NPOS>
+struct Enumerator {
+  uint32_t hm[NPOS > 0 ? NPOS : 1];
+  uint32_t ones;
+  __device__ __forceinline__ explicit Enumerator(const TileGate& g) {
+#pragma unroll
+    for (int j = 0; j < NPOS; ++j) hm[j] = ~((1u << g.pos[j]) - 1u);
+    ones = g.l_ones;
+  }
+  __device__ __forceinline__ uint32_t operator()(uint32_t m) const {
+    uint32_t e = m;
+#pragma unroll
+    for (int j = 0; j < NPOS; ++j) e += e & hm[j];
+    return e | ones;
+  }
+};
+
+template <>
+struct Enumerator<-1> {
+  const uint8_t* pos;
+  int npos;
+  uint32_t ones;
+  __device__ __forceinline__ explicit Enumerator(const TileGate& g) : pos(g.pos), npos(g.npos), ones(g.l_ones) {}
+  __device__ __forceinline__ uint32_t operator()(uint32_t m) const {
+    uint32_t e = m;
+    for (int j = 0; j < npos; ++j) e += e & ~((1u << pos[j]) - 1u);
+    return e | ones;
+  }
+};
+
+// Dispatch on the op's insertion count: 0-3 specialised, more generic.
+#define SPZ_BY_NPOS(npos, CALL) \
+  switch (npos) {               \
+    case 0: CALL(0); break;     \
+    case 1: CALL(1); break;     \
+    case 2: CALL(2); break;     \
+    case 3: CALL(3); break;     \
+    default: CALL(-1); break;   \
+  }
+
+template <int KIND, int NPOS>
 __device__ __forceinline__ void tile_pair(const TileGate& g, double* sre, double* sim, uint32_t npairs) {
+  const Enumerator<NPOS> E(g);
+  const uint32_t tbit = g.tbit;
+  const Coef c = g.c;
   for (uint32_t m = threadIdx.x; m < npairs; m += blockDim.x) {
-    const uint32_t s0 = (uint32_t)deposit(m, g.pos, g.npos) | g.l_ones;
-    const uint32_t s1 = s0 | g.tbit;
-    double a = sre[s0], b = sim[s0], c = sre[s1], d = sim[s1];
-    gate_pair<KIND>(g.c, a, b, c, d);
-    sre[s0] = a; sim[s0] = b; sre[s1] = c; sim[s1] = d;
+    const uint32_t s0 = E(m);
+    const uint32_t s1 = s0 | tbit;
+    double a = sre[s0], b = sim[s0], x = sre[s1], d = sim[s1];
+    if constexpr (KIND >= FK_LAZY_H) fast_pair<KIND>(c, a, b, x, d);
+    else gate_pair<KIND>(c, a, b, x, d);
+    sre[s0] = a; sim[s0] = b; sre[s1] = x; sim[s1] = d;
   }
 }
 
 template <int KIND>
-__device__ __forceinline__ void tile_diag(const TileGate& g, double* sre, double* sim, uint32_t nelem, int global_one) {
+__device__ __forceinline__ void tile_pair_any(const TileGate& g, double* sre, double* sim, uint32_t npairs) {
+#define SPZ_CALL(N) tile_pair<KIND, N>(g, sre, sim, npairs)
+  SPZ_BY_NPOS(g.npos, SPZ_CALL)
+#undef SPZ_CALL
+}
+
+// Fast-mode phase op: per amplitude, a table entry chosen by index parities.
+// The amplitudes visited are the tile's (npos = 0) or, for a local half bit,
+// those with that bit set (inserted by the enumeration).
+// parity(x & mask) = parity(base & mask) ^ parity(e & local part of mask); the
+// first is uniform over the tile.
+template <int NPOS, int PM>
+__device__ __forceinline__ void tile_phase(const TileGate& g, const double2* __restrict__ tab, uint64_t base,
+                                           double* sre, double* sim, uint32_t nelem) {
+  const Enumerator<NPOS> E(g);
+  uint32_t em[PM > 0 ? PM : 1];
+  uint32_t bidx = 0;
+#pragma unroll
+  for (int j = 0; j < PM; ++j) {
+    bidx |= (uint32_t)(__popcll(base & g.pmask[j]) & 1) << j;
+    em[j] = g.pemask[j];
+  }
   for (uint32_t m = threadIdx.x; m < nelem; m += blockDim.x) {
-    const uint32_t e = (uint32_t)deposit(m, g.pos, g.npos) | g.l_ones;
-    const bool one = global_one >= 0 ? global_one != 0 : (e & g.tbit) != 0;
+    const uint32_t e = E(m);
+    uint32_t idx = bidx;
+#pragma unroll
+    for (int j = 0; j < PM; ++j) idx ^= (uint32_t)(__popc(e & em[j]) & 1) << j;
+    const double2 w = __ldg(tab + idx);
+    const double r = sre[e], i = sim[e];
+    sre[e] = dfma(r, w.x, dmul(dneg(i), w.y));
+    sim[e] = dfma(r, w.y, dmul(i, w.x));
+  }
+}
+
+template <int NPOS>
+__device__ __forceinline__ void tile_phase_pm(const TileGate& g, const double2* tab, uint64_t base, double* sre,
+                                              double* sim, uint32_t nelem) {
+  switch (g.pm) {
+    case 0: tile_phase<NPOS, 0>(g, tab, base, sre, sim, nelem); break;
+    case 1: tile_phase<NPOS, 1>(g, tab, base, sre, sim, nelem); break;
+    case 2: tile_phase<NPOS, 2>(g, tab, base, sre, sim, nelem); break;
+    case 3: tile_phase<NPOS, 3>(g, tab, base, sre, sim, nelem); break;
+    case 4: tile_phase<NPOS, 4>(g, tab, base, sre, sim, nelem); break;
+    case 5: tile_phase<NPOS, 5>(g, tab, base, sre, sim, nelem); break;
+    case 6: tile_phase<NPOS, 6>(g, tab, base, sre, sim, nelem); break;
+    case 7: tile_phase<NPOS, 7>(g, tab, base, sre, sim, nelem); break;
+    default: tile_phase<NPOS, kPhaseMaxTerms>(g, tab, base, sre, sim, nelem); break;
+  }
+}
+
+template <int KIND, int NPOS>
+__device__ __forceinline__ void tile_diag(const TileGate& g, double* sre, double* sim, uint32_t nelem, int global_one) {
+  const Enumerator<NPOS> E(g);
+  const uint32_t tbit = g.tbit;
+  const Coef c = g.c;
+  for (uint32_t m = threadIdx.x; m < nelem; m += blockDim.x) {
+    const uint32_t e = E(m);
+    const bool one = global_one >= 0 ? global_one != 0 : (e & tbit) != 0;
     double r = sre[e], i = sim[e];
-    gate_diag<KIND>(g.c, one, r, i);
+    gate_diag<KIND>(c, one, r, i);
     sre[e] = r; sim[e] = i;
   }
 }
 
-__global__ void __launch_bounds__(kTileThreads) tile_kernel(PassArgs A) {
+template <int KIND>
+__device__ __forceinline__ void tile_diag_any(const TileGate& g, double* sre, double* sim, uint32_t nelem,
+                                              int global_one) {
+#define SPZ_CALL(N) tile_diag<KIND, N>(g, sre, sim, nelem, global_one)
+  SPZ_BY_NPOS(g.npos, SPZ_CALL)
+#undef SPZ_CALL
+}
+
+template <int NPOS>
+__device__ __forceinline__ void tile_swap(const TileGate& g, double* sre, double* sim, uint32_t nw) {
+  const Enumerator<NPOS> E(g);
+  const uint32_t t1 = g.tbit, t2 = g.tbit2;
+  for (uint32_t m = threadIdx.x; m < nw; m += blockDim.x) {
+    const uint32_t b0 = E(m);
+    const uint32_t i = b0 | t2, j = b0 | t1;
+    const double r = sre[i], q = sim[i];
+    sre[i] = sre[j]; sim[i] = sim[j];
+    sre[j] = r; sim[j] = q;
+  }
+}
+
+__global__ void __launch_bounds__(kTileThreads, SPZ_TILE_MIN_BLOCKS) tile_kernel(PassArgs A) {
   extern __shared__ double smem[];
   const int K = A.k;
   const uint32_t T = 1u << K;
@@ -118,13 +259,22 @@ __global__ void __launch_bounds__(kTileThreads) tile_kernel(PassArgs A) {
       switch (g.mode) {
         case TM_PAIR:
           switch (g.kind) {
-            case SPZ_GATE_H: tile_pair<SPZ_GATE_H>(g, sre, sim, nw); break;
-            case SPZ_GATE_X: tile_pair<SPZ_GATE_X>(g, sre, sim, nw); break;
-            case SPZ_GATE_Y: tile_pair<SPZ_GATE_Y>(g, sre, sim, nw); break;
-            case SPZ_GATE_RX: tile_pair<SPZ_GATE_RX>(g, sre, sim, nw); break;
-            case SPZ_GATE_RY: tile_pair<SPZ_GATE_RY>(g, sre, sim, nw); break;
-            default: tile_pair<SPZ_GATE_U>(g, sre, sim, nw); break;
+            case SPZ_GATE_H: tile_pair_any<SPZ_GATE_H>(g, sre, sim, nw); break;
+            case SPZ_GATE_X: tile_pair_any<SPZ_GATE_X>(g, sre, sim, nw); break;
+            case SPZ_GATE_Y: tile_pair_any<SPZ_GATE_Y>(g, sre, sim, nw); break;
+            case SPZ_GATE_RX: tile_pair_any<SPZ_GATE_RX>(g, sre, sim, nw); break;
+            case SPZ_GATE_RY: tile_pair_any<SPZ_GATE_RY>(g, sre, sim, nw); break;
+            case FK_LAZY_H: tile_pair_any<FK_LAZY_H>(g, sre, sim, nw); break;
+            case FK_LAZY_RX_A: tile_pair_any<FK_LAZY_RX_A>(g, sre, sim, nw); break;
+            case FK_LAZY_RX_B: tile_pair_any<FK_LAZY_RX_B>(g, sre, sim, nw); break;
+            case FK_LAZY_RY_A: tile_pair_any<FK_LAZY_RY_A>(g, sre, sim, nw); break;
+            case FK_LAZY_RY_B: tile_pair_any<FK_LAZY_RY_B>(g, sre, sim, nw); break;
+            default: tile_pair_any<SPZ_GATE_U>(g, sre, sim, nw); break;
           }
+          break;
+        case TM_PHASE:
+          if (g.npos) tile_phase_pm<1>(g, A.tables + g.ptab, base, sre, sim, nw);
+          else tile_phase_pm<0>(g, A.tables + g.ptab, base, sre, sim, nw);
           break;
         case TM_DIAG_LOCAL:
         case TM_DIAG_GLOBAL: {
@@ -134,21 +284,16 @@ __global__ void __launch_bounds__(kTileThreads) tile_kernel(PassArgs A) {
             if (!gone && g.kind != SPZ_GATE_RZ) break;  // Z / P act on the 1 half only
           }
           switch (g.kind) {
-            case SPZ_GATE_Z: tile_diag<SPZ_GATE_Z>(g, sre, sim, nw, gone); break;
-            case SPZ_GATE_P: tile_diag<SPZ_GATE_P>(g, sre, sim, nw, gone); break;
-            default: tile_diag<SPZ_GATE_RZ>(g, sre, sim, nw, gone); break;
+            case SPZ_GATE_Z: tile_diag_any<SPZ_GATE_Z>(g, sre, sim, nw, gone); break;
+            case SPZ_GATE_P: tile_diag_any<SPZ_GATE_P>(g, sre, sim, nw, gone); break;
+            default: tile_diag_any<SPZ_GATE_RZ>(g, sre, sim, nw, gone); break;
           }
           break;
         }
-        default: {  // TM_SWAP
-          for (uint32_t m = threadIdx.x; m < nw; m += blockDim.x) {
-            const uint32_t b0 = (uint32_t)deposit(m, g.pos, g.npos) | g.l_ones;
-            const uint32_t i = b0 | g.tbit2, j = b0 | g.tbit;
-            const double r = sre[i], q = sim[i];
-            sre[i] = sre[j]; sim[i] = sim[j];
-            sre[j] = r; sim[j] = q;
-          }
-        }
+        default:  // TM_SWAP
+#define SPZ_CALL(N) tile_swap<N>(g, sre, sim, nw)
+          SPZ_BY_NPOS(g.npos, SPZ_CALL)
+#undef SPZ_CALL
       }
       __syncthreads();
     }
@@ -192,18 +337,19 @@ inline int exact_class(int kind) {
 // and diagonally only (controls, and all qubits of diagonal gates).
 inline uint64_t nd_mask(const GateApp& g) {
   if (g.kind == SPZ_GATE_SWAP) return (1ull << g.target) | (1ull << g.target2);
-  if (is_diagonal(g.kind)) return 0;
+  if (is_diagonal(g.kind) || g.kind == FK_PHASE) return 0;
   return 1ull << g.target;
 }
 inline uint64_t d_mask(const GateApp& g) {
-  uint64_t m = g.ones | g.zeros;
+  uint64_t m = g.ones | g.zeros | g.touch;
   if (is_diagonal(g.kind)) m |= 1ull << g.target;
   return m;
 }
 
 // Greedy planner: see the file comment.  `k` local qubits per pass, the low
-// `c` qubits always local.
-std::vector<PlannedPass> plan(const std::vector<GateApp>& gates, uint32_t n, int k, int c) {
+// `c` qubits always local.  With exact = false (fast mode) any two gates that
+// commute mathematically may be swapped.
+std::vector<PlannedPass> plan(const std::vector<GateApp>& gates, uint32_t n, int k, int c, bool exact = true) {
   std::vector<PlannedPass> passes;
   std::vector<GateApp> remaining = gates;
   const uint64_t low = c >= 64 ? ~0ull : ((1ull << c) - 1);
@@ -222,7 +368,7 @@ std::vector<PlannedPass> plan(const std::vector<GateApp>& gates, uint32_t n, int
       const uint64_t nd = nd_mask(g), d = d_mask(g);
       const bool commutes = (nd & (def_nd | def_d)) == 0 && (d & def_nd) == 0;
       const int ec = exact_class(g.kind);
-      const bool exact_ok = ec == EC_PERM || (ec == EC_Y && !def_fma) ||
+      const bool exact_ok = !exact || ec == EC_PERM || (ec == EC_Y && !def_fma) ||
                             (ec == EC_ICOV && !def_icov && !def_fma) ||
                             (ec == EC_FMA && !def_icov && !def_fma && !def_y);
       bool take = false;
@@ -261,13 +407,40 @@ std::vector<PlannedPass> plan(const std::vector<GateApp>& gates, uint32_t n, int
 }
 
 // Build the device description of a gate inside a pass with local qubits `L`.
-TileGate tile_gate(const GateApp& g, const std::vector<int>& local) {
+TileGate tile_gate(const GateApp& g, const std::vector<int>& local, const std::vector<PhaseTable>* tables = nullptr,
+                   const std::vector<uint32_t>* table_offsets = nullptr) {
   int where[64];
   for (int q = 0; q < 64; ++q) where[q] = -1;
   for (size_t j = 0; j < local.size(); ++j) where[local[j]] = (int)j;
   TileGate t{};
   t.kind = g.kind;
   t.c = g.c;
+  if (g.kind == FK_PHASE) {  // elementwise; any qubits (the global index is formed per amplitude)
+    const PhaseTable& tab = (*tables)[g.table];
+    t.mode = TM_PHASE;
+    t.half_bit = tab.half_bit;
+    t.pm = tab.m;
+    for (int j = 0; j < tab.m; ++j) {
+      t.pmask[j] = tab.mask[j];
+      for (int q = 0; q < 64; ++q)
+        if (((tab.mask[j] >> q) & 1) && where[q] >= 0) t.pemask[j] |= 1u << where[q];
+    }
+    t.ptab = (*table_offsets)[g.table];
+    if (tab.half_bit) {
+      // Only the half with the bit set is touched: a local bit is inserted into
+      // the enumeration (every lane busy); a non-local one is a tile predicate.
+      const int q = __builtin_ctzll(tab.half_bit);
+      if (where[q] >= 0) {
+        t.tbit = 1u << where[q];
+        t.l_ones = t.tbit;
+        t.pos[0] = (uint8_t)where[q];
+        t.npos = 1;
+      } else {
+        t.g_ones = tab.half_bit;
+      }
+    }
+    return t;
+  }
   uint32_t l_ones = 0, l_zeros = 0;
   for (int q = 0; q < 64; ++q) {
     const uint64_t b = 1ull << q;
@@ -358,8 +531,8 @@ struct PassTimer {
 
 }  // namespace
 
-std::vector<PlannedPass> plan_passes(const std::vector<GateApp>& gates, uint32_t n, int k, int c) {
-  return plan(gates, n, k, c);
+std::vector<PlannedPass> plan_passes(const std::vector<GateApp>& gates, uint32_t n, int k, int c, bool exact) {
+  return plan(gates, n, k, c, exact);
 }
 
 bool exactly_commuting_kinds(int a, int b) {
@@ -368,13 +541,29 @@ bool exactly_commuting_kinds(int a, int b) {
 }
 
 // Run a list of already validated gate applications on h.
-int run_gates(spz_state_t h, const std::vector<GateApp>& gates, uint32_t flags, spz_exec_stats* st) {
-  if (gates.empty()) return SPZ_OK;
+// FP64-pipe instructions of one executed op (lowered fast ops included).
+uint64_t op_fp64_ops(uint32_t n, const GateApp& g, const std::vector<PhaseTable>& tables) {
+  const uint64_t N = 1ull << n;
+  if (g.kind >= FK_LAZY_H && g.kind <= FK_LAZY_RY_B) return 4 * (N / 2);
+  if (g.kind == FK_PHASE) return tables[g.table].half_bit ? 4 * (N / 2) : 4 * N;
+  return gate_fp64_ops(n, g);
+}
+
+// Run a list of already validated gate applications on h.
+int run_gates(spz_state_t h, const std::vector<GateApp>& gates_in, uint32_t flags, spz_exec_stats* st) {
+  if (gates_in.empty()) return SPZ_OK;
   const uint32_t n = h->n;
+  const bool fast = (flags & SPZ_EXEC_FAST) != 0;
+  std::vector<GateApp> lowered;
+  std::vector<PhaseTable> tables;
+  if (fast) lower_fast(gates_in, n, &lowered, &tables);
+  const std::vector<GateApp>& gates = fast ? lowered : gates_in;
+  if (st)
+    for (const GateApp& g : gates) st->fp64_ops += op_fp64_ops(n, g, tables);
   PassTimer timer;
   timer.on = (flags & SPZ_EXEC_TIME_PASSES) != 0;
   timer.stream = h->stream;
-  if (flags & SPZ_EXEC_UNFUSED) {
+  if ((flags & SPZ_EXEC_UNFUSED) && !fast) {
     for (const GateApp& g : gates) {
       int rc = timer.begin();
       if (!rc) rc = launch_gate(h, g);
@@ -392,35 +581,61 @@ int run_gates(spz_state_t h, const std::vector<GateApp>& gates, uint32_t flags, 
   }
   const int k = std::min<int>((int)n, kTileMaxK);
   const int c = std::min<int>(kTileLowBits, k);
-  std::vector<PlannedPass> passes = plan(gates, n, k, c);
-  // Upload every tile gate of every fused pass in one copy.
+  std::vector<PlannedPass> passes = plan(gates, n, k, c, !fast);
+  // Phase tables, flattened (re, im) after the gate list.
+  std::vector<uint32_t> table_offsets;
+  std::vector<double> flat;
+  for (const PhaseTable& t : tables) {
+    table_offsets.push_back((uint32_t)(flat.size() / 2));
+    for (size_t i = 0; i < t.re.size(); ++i) {
+      flat.push_back(t.re[i]);
+      flat.push_back(t.im[i]);
+    }
+  }
+  // A pass runs as a tile pass unless it is one exact gate (the plain kernel
+  // touches only what that gate needs); lowered fast ops exist only in tiles.
+  auto tiled = [&](const PlannedPass& P) {
+    return P.gates.size() > 1 || P.gates[0].kind >= FK_LAZY_H;
+  };
   std::vector<TileGate> all;
   std::vector<size_t> offs;
   for (const PlannedPass& P : passes) {
     offs.push_back(all.size());
-    if (P.gates.size() > 1)
-      for (const GateApp& g : P.gates) all.push_back(tile_gate(g, P.local));
+    if (tiled(P))
+      for (const GateApp& g : P.gates) all.push_back(tile_gate(g, P.local, &tables, &table_offsets));
   }
   TileGate* dgates = nullptr;
+  const double2* dtables = nullptr;
   if (!all.empty()) {
     void* dscr;
-    const size_t bytes = all.size() * sizeof(TileGate);
-    int rc = ensure_dev_scratch(h, bytes, &dscr);
+    const size_t gbytes = (all.size() * sizeof(TileGate) + 255) / 256 * 256;
+    const size_t tbytes = flat.size() * sizeof(double);
+    int rc = ensure_dev_scratch(h, gbytes + tbytes, &dscr);
     if (rc) return rc;
     // From pageable memory: the runtime stages the bytes before returning, so
-    // `all` may go out of scope while the copy is still queued on the stream.
-    SPZ_CUDA(cudaMemcpyAsync(dscr, all.data(), bytes, cudaMemcpyHostToDevice, h->stream));
+    // `all` and `flat` may go out of scope while the copies are still queued.
+    SPZ_CUDA(cudaMemcpyAsync(dscr, all.data(), all.size() * sizeof(TileGate), cudaMemcpyHostToDevice, h->stream));
+    if (tbytes)
+      SPZ_CUDA(cudaMemcpyAsync((char*)dscr + gbytes, flat.data(), tbytes, cudaMemcpyHostToDevice, h->stream));
     dgates = (TileGate*)dscr;
+    dtables = (const double2*)((char*)dscr + gbytes);
   }
-  static bool attr_set = false;
-  if (!attr_set) {
-    SPZ_CUDA(cudaFuncSetAttribute(tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (2 << kTileMaxK) * 8 + (1 << kTileMaxK) * 8));
-    attr_set = true;
+  // Resident blocks per SM for the full-size tile; the grid is one wave of them
+  // (each block loops over tiles), so no block waits for a second wave.
+  static int resident = 0, sms = kNumSMs;
+  if (!resident) {
+    SPZ_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device));
+    const int max_smem = (2 << kTileMaxK) * 8 + (1 << (kTileMaxK - kTileLowBits)) * 8;
+    SPZ_CUDA(cudaFuncSetAttribute(tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+    SPZ_CUDA(cudaFuncSetAttribute(tile_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                  cudaSharedmemCarveoutMaxShared));
+    int per_sm = 0;
+    SPZ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tile_kernel, kTileThreads, max_smem));
+    resident = std::max(1, per_sm);
   }
   for (size_t p = 0; p < passes.size(); ++p) {
     const PlannedPass& P = passes[p];
-    if (P.gates.size() == 1) {  // a lone gate: the plain kernel touches only what it needs
+    if (!tiled(P)) {
       int rc = timer.begin();
       if (!rc) rc = launch_gate(h, P.gates[0]);
       if (!rc) rc = timer.end(false);
@@ -443,11 +658,12 @@ int run_gates(spz_state_t h, const std::vector<GateApp>& gates, uint32_t flags, 
     for (int j = 0; j < A.k; ++j) A.lpos[j] = (uint8_t)P.local[j];
     A.ntiles = 1ull << (n - A.k);
     A.gates = dgates + offs[p];
+    A.tables = dtables;
     A.ngates = (int)P.gates.size();
     const uint32_t T = 1u << A.k;
     const size_t smem = 2 * T * sizeof(double) + (size_t)(1u << A.nhigh) * sizeof(uint64_t);
     const int threads = (int)std::min<uint32_t>(kTileThreads, std::max<uint32_t>(32, T / 2));
-    const uint64_t blocks = std::min<uint64_t>(A.ntiles, (uint64_t)kNumSMs * 4);
+    const uint64_t blocks = std::min<uint64_t>(A.ntiles, (uint64_t)sms * resident);
     int rc = timer.begin();
     if (rc) {
       timer.collect(nullptr);
@@ -555,7 +771,6 @@ int execute(spz_state_t h, const spz_op* ops, size_t nops, spz_tracker* tracker,
     if (st) {
       st->gates++;
       st->algorithmic_bytes += gate_algorithmic_bytes(h->n, a);
-      st->fp64_ops += gate_fp64_ops(h->n, a);
     }
   }
   int rc = run_gates(h, seg, flags, st);
@@ -574,7 +789,13 @@ int plan_stats(uint32_t n, const spz_op* ops, size_t nops, uint32_t flags, spz_e
   std::vector<GateApp> seg;
   auto flush = [&]() {
     if (seg.empty()) return;
-    if (flags & SPZ_EXEC_UNFUSED) {
+    const bool fast = (flags & SPZ_EXEC_FAST) != 0;
+    std::vector<GateApp> lowered;
+    std::vector<PhaseTable> tables;
+    if (fast) lower_fast(seg, n, &lowered, &tables);
+    const std::vector<GateApp>& run = fast ? lowered : seg;
+    for (const GateApp& g : run) st->fp64_ops += op_fp64_ops(n, g, tables);
+    if ((flags & SPZ_EXEC_UNFUSED) && !fast) {
       for (const GateApp& g : seg) {
         if (order) {
           order->push_back((uint32_t)g.src);
@@ -586,14 +807,14 @@ int plan_stats(uint32_t n, const spz_op* ops, size_t nops, uint32_t flags, spz_e
     } else {
       const int k = std::min<int>((int)n, kTileMaxK);
       const int c = std::min<int>(kTileLowBits, k);
-      for (const PlannedPass& P : plan(seg, n, k, c)) {
-        if (order)
+      for (const PlannedPass& P : plan(run, n, k, c, !fast)) {
+        if (order && !fast)
           for (const GateApp& g : P.gates) {
             order->push_back((uint32_t)g.src);
             pass_of->push_back((uint32_t)st->passes);
           }
         st->passes++;
-        if (P.gates.size() > 1) {
+        if (P.gates.size() > 1 || P.gates[0].kind >= FK_LAZY_H) {
           st->tile_passes++;
           st->bytes_moved += 32ull << n;
         } else {
@@ -628,7 +849,6 @@ int plan_stats(uint32_t n, const spz_op* ops, size_t nops, uint32_t flags, spz_e
     seg.push_back(a);
     st->gates++;
     st->algorithmic_bytes += gate_algorithmic_bytes(n, a);
-    st->fp64_ops += gate_fp64_ops(n, a);
   }
   flush();
   return SPZ_OK;

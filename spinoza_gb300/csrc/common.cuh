@@ -108,6 +108,30 @@ struct Coef {
 
 int coef_for(const spz_gate& g, Coef* out);
 
+// Ops produced by the fast-mode lowering (fast.cu); they exist only inside the
+// fused executor.  Lazy ops are a gate divided by a scalar that is carried in
+// the executor's global factor; phase ops multiply amplitudes by table entries
+// selected by parities of index bits.
+enum FastKind {
+  FK_LAZY_H = 100,     // [[1, 1], [1, -1]]                (H = 2^-1/2 x this)
+  FK_LAZY_RX_A = 101,  // [[1, -i t], [-i t, 1]], t = tan  (RX = cos x this)
+  FK_LAZY_RX_B = 102,  // [[u, -i], [-i, u]],     u = cot  (RX = sin x this)
+  FK_LAZY_RY_A = 103,  // [[1, -t], [t, 1]]                (RY = cos x this)
+  FK_LAZY_RY_B = 104,  // [[u, -1], [1, u]]                (RY = sin x this)
+  FK_PHASE = 105       // x -> table[parities of x & mask_j] x (only where x & half_bit, if set)
+};
+
+constexpr int kPhaseMaxTerms = 8;
+
+// One phase op: 2^m complex entries indexed by the parities of the index under
+// m masks; applied to every amplitude, or only to those with half_bit set.
+struct PhaseTable {
+  int m = 0;
+  uint64_t mask[kPhaseMaxTerms] = {};
+  uint64_t half_bit = 0;
+  std::vector<double> re, im;  // 2^m entries
+};
+
 // Validated, normalised description of one gate application.
 struct GateApp {
   int kind;          // enum spz_gate_kind (H,X,Y,Z,P,RX,RY,RZ,U,SWAP)
@@ -117,7 +141,14 @@ struct GateApp {
   uint64_t zeros;    // controls that must read 0
   Coef c;
   int64_t src = -1;  // index of the circuit op it came from (planning reports)
+  int32_t table = -1;  // FK_PHASE: index of its PhaseTable
+  uint64_t touch = 0;  // FK_PHASE: qubits its phases depend on (diagonal action)
 };
+
+// Fast-mode lowering (fast.cu): rewrite `in` into lazy ops, phase ops and
+// exact gates with the same overall action (up to rounding).
+void lower_fast(const std::vector<GateApp>& in, uint32_t n, std::vector<GateApp>* out,
+                std::vector<PhaseTable>* tables);
 
 // Validate and build a GateApp (returns a status).
 int make_gate_app(uint32_t n, const spz_gate& g, uint32_t target, uint64_t ones, uint64_t zeros,
@@ -142,7 +173,8 @@ struct PlannedPass {
   std::vector<int> local;  // sorted local qubits
   std::vector<GateApp> gates;
 };
-std::vector<PlannedPass> plan_passes(const std::vector<GateApp>& gates, uint32_t n, int k, int c);
+// exact: reorder only gates whose exchange is bit-identical (else any that commute).
+std::vector<PlannedPass> plan_passes(const std::vector<GateApp>& gates, uint32_t n, int k, int c, bool exact = true);
 
 // Reductions used by measurement and the executor.
 int prob0_device(spz_state_t h, uint32_t target, double* out);

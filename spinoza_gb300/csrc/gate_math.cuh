@@ -63,6 +63,26 @@ __device__ __forceinline__ void gate_pair(const Coef& g, double& a, double& b, d
   }
 }
 
+// Fast-mode lazy ops (the gate divided by a scalar carried elsewhere): four
+// FP64 instructions per pair.  Coefficient in g.cs (t or u).
+template <int FK>
+__device__ __forceinline__ void fast_pair(const Coef& g, double& a, double& b, double& c, double& d) {
+  const double t = g.cs;
+  double na, nb, nc, nd;
+  if constexpr (FK == FK_LAZY_H) {
+    na = dadd(a, c); nb = dadd(b, d); nc = dsub(a, c); nd = dsub(b, d);
+  } else if constexpr (FK == FK_LAZY_RX_A) {  // s0 - i t s1, -i t s0 + s1
+    na = dfma(t, d, a); nb = dfma(dneg(t), c, b); nc = dfma(t, b, c); nd = dfma(dneg(t), a, d);
+  } else if constexpr (FK == FK_LAZY_RX_B) {  // u s0 - i s1, -i s0 + u s1
+    na = dfma(t, a, d); nb = dfma(t, b, dneg(c)); nc = dfma(t, c, b); nd = dfma(t, d, dneg(a));
+  } else if constexpr (FK == FK_LAZY_RY_A) {  // s0 - t s1, t s0 + s1
+    na = dfma(dneg(t), c, a); nb = dfma(dneg(t), d, b); nc = dfma(t, a, c); nd = dfma(t, b, d);
+  } else {  // FK_LAZY_RY_B: u s0 - s1, s0 + u s1
+    na = dfma(t, a, dneg(c)); nb = dfma(t, b, dneg(d)); nc = dfma(t, c, a); nd = dfma(t, d, b);
+  }
+  a = na; b = nb; c = nc; d = nd;
+}
+
 // Diagonal gates on one amplitude; `one` is the amplitude's target bit.
 template <int KIND>
 __device__ __forceinline__ void gate_diag(const Coef& g, bool one, double& re, double& im) {

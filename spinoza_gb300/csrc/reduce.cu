@@ -258,12 +258,278 @@ __global__ void __launch_bounds__(kRedThreads) x_pauli_kernel(const double* __re
   if (threadIdx.x == 0) partials[blockIdx.x] = s;
 }
 
+// ------------------------------------------------ fused Pauli-sum tile passes
+// One pass loads a tile of 2^k amplitudes (all values of k local qubits) into
+// shared memory and accumulates, per thread:
+//  * (first pass only) the diagonal terms: with w_k = parity(x & z_k), the
+//    diagonal part is D(x) = C + sum_j T_j[w bits 8j..8j+7], T_j 256-entry tables
+//    of -2 sum c_k over the set bits, so a whole Ising-type chain costs a few
+//    FP64 operations per amplitude; energy += |psi_x|^2 D(x);
+//  * every X/Y-type term whose X-mask lies in the tile: per pair (x, x ^ xmask)
+//    the pair's contribution to Re<psi|P|psi>, one accumulator per term.
+// Each term's accumulators are reduced once at the end (fixed order).
+constexpr int kPtMaxTerms = 16;   // X-type terms per pass
+constexpr int kPtMaxDiag = 64;    // diagonal terms (8 chunks of 8)
+constexpr int kPtK = 12, kPtLow = 3, kPtThreads = 512;
+
+struct PtTerm {
+  uint32_t xl;      // X-mask in local bits
+  int32_t lowbit;   // lowest bit of xl
+  uint64_t z;       // Z-mask (qubits)
+  int32_t ny;       // Y count
+  int32_t simple;   // pure X string (z = 0, ny = 0): 2 Re w
+};
+
+struct PtArgs {
+  const double* re;
+  const double* im;
+  uint64_t ntiles;
+  int k, c, nhigh;
+  uint8_t lpos[kPtK];
+  int ndiag;                 // diagonal terms handled in this pass (0 or all)
+  uint64_t dz[kPtMaxDiag];   // their Z-masks
+  const double* dtab;        // nchunks x 256 table entries
+  double dconst;             // C = sum of the diagonal coefficients
+  int nt;
+  PtTerm t[kPtMaxTerms];
+  double* partials;          // (nt + 1) x gridDim.x
+};
+
+__global__ void __launch_bounds__(kPtThreads) pauli_tile_kernel(PtArgs A) {
+  extern __shared__ double sm[];
+  const uint32_t T = 1u << A.k;
+  double* sre = sm;
+  double* sim = sm + T;
+  uint64_t* rowoff = reinterpret_cast<uint64_t*>(sm + 2 * T);
+  double* red = sm + 2 * T + (T >> kPtLow) + 1;
+  const uint32_t cmask = (1u << A.c) - 1;
+  for (uint32_t r = threadIdx.x; r < (1u << A.nhigh); r += blockDim.x) {
+    uint64_t off = 0;
+    for (int j = 0; j < A.nhigh; ++j)
+      if ((r >> j) & 1) off |= 1ull << A.lpos[A.c + j];
+    rowoff[r] = off;
+  }
+  double acc[kPtMaxTerms + 1];
+#pragma unroll
+  for (int j = 0; j <= kPtMaxTerms; ++j) acc[j] = 0.0;
+  __syncthreads();
+  for (uint64_t tile = blockIdx.x; tile < A.ntiles; tile += gridDim.x) {
+    const uint64_t base = deposit(tile, A.lpos, A.k);
+    for (uint32_t e2 = threadIdx.x; e2 < T / 2; e2 += blockDim.x) {
+      const uint32_t e = 2 * e2;
+      const uint64_t gi = base | rowoff[e >> A.c] | (e & cmask);
+      *reinterpret_cast<double2*>(sre + e) = *reinterpret_cast<const double2*>(A.re + gi);
+      *reinterpret_cast<double2*>(sim + e) = *reinterpret_cast<const double2*>(A.im + gi);
+    }
+    __syncthreads();
+    if (A.ndiag) {
+      for (uint32_t e = threadIdx.x; e < T; e += blockDim.x) {
+        const uint64_t gi = base | rowoff[e >> A.c] | (e & cmask);
+        double d = A.dconst;
+        for (int j0 = 0; j0 < A.ndiag; j0 += 8) {
+          uint32_t w = 0;
+          const int jn = min(8, A.ndiag - j0);
+          for (int j = 0; j < jn; ++j) w |= (uint32_t)(__popcll(gi & A.dz[j0 + j]) & 1) << j;
+          d = dadd(d, A.dtab[(j0 / 8) * 256 + w]);
+        }
+        const double a = sre[e], b = sim[e];
+        acc[kPtMaxTerms] = dfma(dfma(a, a, dmul(b, b)), d, acc[kPtMaxTerms]);
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < kPtMaxTerms; ++t) {
+      if (t >= A.nt) break;
+      const PtTerm P = A.t[t];
+      const uint32_t lowmask = (1u << P.lowbit) - 1;
+      for (uint32_t m = threadIdx.x; m < T / 2; m += blockDim.x) {
+        const uint32_t x = ((m & ~lowmask) << 1) | (m & lowmask);
+        const uint32_t y = x ^ P.xl;
+        const double a = sre[x], b = sim[x], c = sre[y], d = sim[y];
+        if (P.simple) {  // 2 Re(conj(psi_x) psi_y); the factor 2 is applied at the end
+          acc[t] = dfma(a, c, acc[t]);
+          acc[t] = dfma(b, d, acc[t]);
+        } else {
+          const uint64_t gx = base | rowoff[x >> A.c] | (x & cmask);
+          const uint64_t gy = base | rowoff[y >> A.c] | (y & cmask);
+          const int sx = (__popcll(gx & P.z) & 1) ? -1 : 1;
+          const int sy = (__popcll(gy & P.z) & 1) ? -1 : 1;
+          const int ny = P.ny & 3;
+          const double wre = dfma(a, c, dmul(b, d)), wim = dfma(a, d, dmul(dneg(b), c));
+          int f;
+          double v;
+          if ((ny & 1) == 0) {
+            f = (sx + sy) * (ny == 0 ? 1 : -1);
+            v = wre;
+          } else {
+            f = (sy - sx) * (ny == 1 ? -1 : 1);
+            v = wim;
+          }
+          // half of f * v (f is -2, 0 or 2): the factor 2 is applied at the end
+          if (f > 0) acc[t] = dadd(acc[t], v);
+          else if (f < 0) acc[t] = dsub(acc[t], v);
+        }
+      }
+    }
+    __syncthreads();
+  }
+  // one fixed-order block reduction per accumulator; row t < nt: term t, row nt: diagonal
+#pragma unroll
+  for (int s = 0; s <= kPtMaxTerms; ++s) {
+    if (s < kPtMaxTerms && s >= A.nt) continue;
+    const int row = s == kPtMaxTerms ? A.nt : s;
+    double v = acc[s];
+    for (int off = 16; off > 0; off >>= 1) v = dadd(v, __shfl_down_sync(0xffffffffu, v, off));
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+      double r = lane < (int)(blockDim.x >> 5) ? red[lane] : 0.0;
+      for (int off = 16; off > 0; off >>= 1) r = dadd(r, __shfl_down_sync(0xffffffffu, r, off));
+      if (lane == 0) A.partials[(size_t)row * gridDim.x + blockIdx.x] = r;
+    }
+    __syncthreads();
+  }
+}
+
+// Tile-pass evaluation; returns false (nothing launched) when the terms do not
+// fit its limits, so the caller uses the per-group kernels.
+static int pauli_tiles(spz_state_t h, const spz_pauli_term* terms, size_t nterms, double* out, bool* done) {
+  *done = false;
+  const uint32_t n = h->n;
+  const int k = std::min<int>((int)n, kPtK);
+  const int c = std::min<int>(kPtLow, k);
+  std::vector<size_t> diag, xt;
+  for (size_t i = 0; i < nterms; ++i) (terms[i].x_mask ? xt : diag).push_back(i);
+  if (diag.size() > (size_t)kPtMaxDiag) return SPZ_OK;
+  for (size_t i : xt)
+    if (__builtin_popcountll(terms[i].x_mask) > k - c) return SPZ_OK;
+  // passes: greedy local sets covering the X-masks
+  struct Pass { std::vector<int> local; std::vector<size_t> terms; bool diag; };
+  std::vector<Pass> passes;
+  std::vector<int> done_t(xt.size(), 0);
+  size_t left = xt.size();
+  bool first = true;
+  while (left > 0 || first) {
+    uint64_t L = (1ull << c) - 1;
+    int nl = c;
+    Pass P;
+    P.diag = first && !diag.empty();
+    for (size_t j = 0; j < xt.size() && (int)P.terms.size() < kPtMaxTerms; ++j) {
+      if (done_t[j]) continue;
+      const uint64_t need = terms[xt[j]].x_mask & ~L;
+      const int add = __builtin_popcountll(need);
+      if (nl + add <= k) {
+        L |= need;
+        nl += add;
+        P.terms.push_back(xt[j]);
+        done_t[j] = 1;
+        left--;
+      }
+    }
+    for (int q = 0; q < (int)n && nl < k; ++q)
+      if (!((L >> q) & 1)) { L |= 1ull << q; nl++; }
+    for (int q = 0; q < (int)n; ++q)
+      if ((L >> q) & 1) P.local.push_back(q);
+    first = false;
+    if (P.diag || !P.terms.empty()) passes.push_back(std::move(P));
+    if (left == 0) break;
+  }
+  // diagonal tables
+  const size_t nd = diag.size();
+  const size_t nchunks = (nd + 7) / 8;
+  std::vector<double> tab(std::max<size_t>(1, nchunks) * 256, 0.0);
+  double dconst = 0.0;
+  for (size_t j = 0; j < nd; ++j) dconst += terms[diag[j]].coeff;
+  for (size_t ch = 0; ch < nchunks; ++ch)
+    for (int v = 0; v < 256; ++v) {
+      double s = 0.0;
+      for (int b = 0; b < 8 && ch * 8 + b < nd; ++b)
+        if ((v >> b) & 1) s += -2.0 * terms[diag[ch * 8 + b]].coeff;
+      tab[ch * 256 + v] = s;
+    }
+  const int blocks = (int)std::min<uint64_t>(1ull << (n - k), (uint64_t)kNumSMs * 3);
+  const size_t slots_per_pass = (size_t)(kPtMaxTerms + 1) * blocks;
+  const size_t nres = passes.size() * (kPtMaxTerms + 1);
+  void* scratch;
+  int rc = ensure_dev_scratch(h, (tab.size() + passes.size() * slots_per_pass + nres) * sizeof(double), &scratch);
+  if (rc) return rc;
+  double* dtab = (double*)scratch;
+  double* dpart = dtab + tab.size();
+  double* dres = dpart + passes.size() * slots_per_pass;
+  SPZ_CUDA(cudaMemcpyAsync(dtab, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  static bool attr = false;
+  if (!attr) {
+    SPZ_CUDA(cudaFuncSetAttribute(pauli_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)((2 << kPtK) + (1 << (kPtK - kPtLow)) + 64) * 8));
+    attr = true;
+  }
+  for (size_t p = 0; p < passes.size(); ++p) {
+    const Pass& P = passes[p];
+    PtArgs A{};
+    A.re = h->re;
+    A.im = h->im;
+    A.k = (int)P.local.size();
+    A.c = c;
+    A.nhigh = A.k - c;
+    for (int j = 0; j < A.k; ++j) A.lpos[j] = (uint8_t)P.local[j];
+    A.ntiles = 1ull << (n - A.k);
+    int where[64];
+    for (int q = 0; q < 64; ++q) where[q] = -1;
+    for (size_t j = 0; j < P.local.size(); ++j) where[P.local[j]] = (int)j;
+    if (P.diag) {
+      A.ndiag = (int)nd;
+      for (size_t j = 0; j < nd; ++j) A.dz[j] = terms[diag[j]].z_mask;
+      A.dtab = dtab;
+      A.dconst = dconst;
+    }
+    A.nt = (int)P.terms.size();
+    for (int t = 0; t < A.nt; ++t) {
+      const spz_pauli_term& tm = terms[P.terms[t]];
+      PtTerm& pt = A.t[t];
+      for (int q = 0; q < 64; ++q)
+        if ((tm.x_mask >> q) & 1) pt.xl |= 1u << where[q];
+      pt.lowbit = __builtin_ctz(pt.xl);
+      pt.z = tm.z_mask;
+      pt.ny = __builtin_popcountll(tm.x_mask & tm.z_mask);
+      pt.simple = tm.z_mask == 0;
+    }
+    A.partials = dpart + p * slots_per_pass;
+    const uint32_t T = 1u << A.k;
+    const size_t smem = (2 * T + (T >> kPtLow) + 1 + 32) * sizeof(double);
+    const int threads = (int)std::min<uint32_t>(kPtThreads, std::max<uint32_t>(32, T / 2));
+    const int nb = (int)std::min<uint64_t>(A.ntiles, (uint64_t)blocks);
+    pauli_tile_kernel<<<nb, threads, smem, h->stream>>>(A);
+    finalize_kernel<<<1, 1024, 0, h->stream>>>(A.partials, nb, A.nt + 1, dres + p * (kPtMaxTerms + 1));
+    SPZ_CHECK_LAUNCH("pauli_tile_kernel");
+  }
+  std::vector<double> res(nres);
+  rc = read_back(h, dres, res.data(), nres);
+  if (rc) return rc;
+  double total = 0.0;
+  for (size_t p = 0; p < passes.size(); ++p) {
+    const Pass& P = passes[p];
+    const double* r = res.data() + p * (kPtMaxTerms + 1);
+    for (size_t t = 0; t < P.terms.size(); ++t) total += terms[P.terms[t]].coeff * 2.0 * r[t];
+    if (P.diag) total += r[P.terms.size()];
+  }
+  *out = total;
+  *done = true;
+  return SPZ_OK;
+}
+
 int pauli_expectation(spz_state_t h, const spz_pauli_term* terms, size_t nterms, double* out) {
   if (nterms && !terms) return fail(SPZ_ERR_NULL, "terms is NULL");
   for (size_t k = 0; k < nterms; ++k)
     if (h->n < 64 && ((terms[k].x_mask | terms[k].z_mask) >> h->n) != 0)
       return fail(SPZ_ERR_INVALID_ARGUMENT, "Pauli term acts on a qubit out of range");
-  // Group: diagonal terms, then one group per distinct x_mask (chunks of 64 terms).
+  if (nterms == 0) {
+    *out = 0.0;
+    return SPZ_OK;
+  }
+  bool done = false;
+  int rc0 = pauli_tiles(h, terms, nterms, out, &done);
+  if (rc0 || done) return rc0;
+  // Fallback: diagonal terms, then one pass per distinct x_mask (chunks of 64 terms).
   std::vector<std::vector<size_t>> groups;
   std::vector<uint64_t> group_x;
   for (size_t k = 0; k < nterms; ++k) {

@@ -22,14 +22,20 @@ _NAMES = {nat.H: "H", nat.M: "M", nat.X: "X", nat.Y: "Y", nat.Z: "Z", nat.P: "P"
 
 
 class Gate:
-    __slots__ = ("kind", "params", "qubits")
+    __slots__ = ("kind", "params", "qubits", "matrix")
 
-    def __init__(self, kind: int, params: Sequence[float] = (), qubits: Sequence[int] = ()):
+    def __init__(self, kind: int, params: Sequence[float] = (), qubits: Sequence[int] = (), matrix=None):
         self.kind = int(kind)
         p = [float(v) for v in params] + [0.0] * (3 - len(params))
         self.params = tuple(p[:3])
         q = [int(v) for v in qubits] + [0] * (2 - len(qubits))
         self.qubits = tuple(q[:2])
+        self.matrix = matrix  # Unitary payload (gates.rs:67)
+
+    @staticmethod
+    def Unitary(u) -> "Gate":
+        """A dense unitary (spinoza_gb300.unitaries.Unitary) acting on qubits target .. target+m-1."""
+        return Gate(nat.UNITARY, matrix=u)
 
     # payload variants
     @staticmethod
@@ -89,6 +95,12 @@ class Gate:
         if k == nat.U:
             t, p, l = self.params
             return Gate(nat.U, (-t, -l, -p))
+        if k == nat.UNITARY:  # gates.rs:87-90: conjugate transpose
+            from .unitaries import Unitary
+
+            u = Unitary(self.matrix.reals.copy(), self.matrix.imags.copy(), self.matrix.height, self.matrix.width)
+            u.conj_t()
+            return Gate.Unitary(u)
         raise nat.Unsupported(nat.SPZ_ERR_UNSUPPORTED, f"{self!r} has no inverse (gates.rs:86)")
 
     def to_matrix(self) -> np.ndarray:
@@ -155,12 +167,22 @@ def _resolve(gate: Gate) -> nat.spz_gate:
 
 def apply(gate: Gate, state: State, target: int) -> None:
     """Uncontrolled gate on `target` (gates.rs:215-232)."""
+    if gate.kind == nat.UNITARY:
+        from .unitaries import transform_u
+
+        transform_u(state, gate.matrix, target)
+        return
     g = _resolve(gate)
     nat.check(nat.lib().spz_apply(state.handle, nat.byref(g), int(target)))
 
 
 def c_apply(gate: Gate, state: State, control: int, target: int) -> None:
     """Gate on `target` where `control` reads 1 (gates.rs:257-269)."""
+    if gate.kind == nat.UNITARY:
+        from .unitaries import c_transform_u
+
+        c_transform_u(state, gate.matrix, control, target)
+        return
     g = gate.c_struct()
     nat.check(nat.lib().spz_c_apply(state.handle, nat.byref(g), int(control), int(target)))
 

@@ -54,6 +54,28 @@ def test_pauli_sum_matches_oracle(gpu, n):
     assert abs(got - want) < 1e-12 * max(1.0, abs(want))
 
 
+@pytest.mark.parametrize("n", [2, 7, 14, 19])
+def test_pauli_sum_tile_path(gpu, n):
+    """Terms that fit the fused tile passes: X/Y masks of up to 3 qubits, any Z
+    mask, identity terms, and more than 8 diagonal terms (several chunks)."""
+    re, im = rng.normal_state(n, 40 + n)
+    s = State.from_arrays(re, im)
+    r = np.random.default_rng(100 + n)
+    terms = [(0.5, 0, 0)]
+    for _ in range(30):
+        z = int(r.integers(0, 1 << n))
+        terms.append((float(r.normal()), 0, z))
+    for _ in range(40):
+        qs = r.choice(n, size=min(n, int(r.integers(1, 4))), replace=False)
+        x = sum(1 << int(q) for q in qs)
+        z = int(r.integers(0, 1 << n)) if r.random() < 0.5 else 0
+        terms.append((float(r.normal()), x, z))
+    arr = core.pauli_terms(terms)
+    got = core.pauli_expectation(s, arr)
+    want = oracle.pauli_expectation(re, im, arr)
+    assert abs(got - want) < 1e-12 * max(1.0, sum(abs(t[0]) for t in terms))
+
+
 def test_ising_hamiltonian_config3_form(gpu):
     n = 16
     re, im = rng.normal_state(n, 3)

@@ -159,6 +159,19 @@ def test_planner_schedule_brickwork_and_qft_bit_exact(native):
         assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
 
 
+def test_fast_lowering_cuts_fp64_instructions(native):
+    """Fast mode: U as P RY P with lazy scaling and phases pushed through the CX
+    ladders needs ~8 instead of 14 FP64 instructions per pair and gate."""
+    ops = brickwork_ops(30, 20)
+    exact = circuit.plan_stats(30, ops)
+    fast = circuit.plan_stats(30, ops, fast=True)
+    assert exact["fp64_ops"] == 600 * 14 * (1 << 29)
+    assert fast["fp64_ops"] < 0.6 * exact["fp64_ops"]
+    assert fast["gates"] == exact["gates"] and fast["algorithmic_bytes"] == exact["algorithmic_bytes"]
+    q = circuit.plan_stats(20, qft_ops(20), fast=True)
+    assert q["fp64_ops"] < circuit.plan_stats(20, qft_ops(20))["fp64_ops"]
+
+
 def test_planner_measurement_is_a_barrier(native):
     ops = np.zeros(3, dtype=nat.OP_DTYPE)
     ops[0] = ((nat.H, 0, 0, 0, (0, 0, 0)), 0, 0, 0, 0)

@@ -1,0 +1,109 @@
+"""OpenQASM 2.0 front-end (openqasm.rs): parsing on the host; execution parity
+on the GPU against the same circuit built with the builders (openqasm.rs:174-305
+compare loaded programs with builder circuits)."""
+import math
+
+import numpy as np
+import pytest
+
+from spinoza_gb300 import openqasm
+from spinoza_gb300.circuit import QuantumCircuit, QuantumRegister
+
+IQFT4 = """OPENQASM 2.0;
+include "qelib1.inc";
+qreg q[4];
+h q[0];
+cp(-pi/2) q[0],q[1];
+cp(-pi/4) q[0],q[2];
+cp(-pi/8) q[0],q[3];
+h q[1];
+cp(-pi/2) q[1],q[2];
+cp(-pi/4) q[1],q[3];
+h q[2];
+cp(-pi/2) q[2],q[3];
+h q[3];
+"""
+
+NONCONTROLLED8 = """OPENQASM 2.0;
+qreg q[8];
+h q[0]; x q[1]; y q[2]; z q[3];
+rx(1.0) q[4]; ry(2.0) q[5]; rz(3.0) q[6];
+u(1.0,2.0,3.0) q[7];
+"""
+
+TWO_REGS = """OPENQASM 2.0;
+qreg a[2];
+qreg b[3];
+creg c[3];
+h a;            // broadcast over the register
+cx a[1], b[0];
+ccx a[0], a[1], b[2];
+crz(pi/3) b[0], b[1];
+swap a[0], b[1];
+barrier a, b;
+measure b[2] -> c[2];
+"""
+
+
+def _kinds(qc):
+    return [(t.gate.kind, t.target, t.controls.kind, tuple(t.controls.controls)) for t in qc.transformations]
+
+
+def test_parse_matches_builder_iqft():
+    qc = openqasm.loads(IQFT4)
+    ref = QuantumCircuit(QuantumRegister(4))
+    ref.iqft([3, 2, 1, 0])
+    assert _kinds(qc) == _kinds(ref)
+    got = [t.gate.params for t in qc.transformations]
+    want = [t.gate.params for t in ref.transformations]
+    assert got == want
+
+
+def test_parse_two_registers_and_broadcast():
+    qc = openqasm.loads(TWO_REGS)
+    assert qc.num_qubits == 5 and qc.quantum_registers_info == [2, 3]
+    names = [(t.gate.kind, t.target, tuple(t.controls.controls)) for t in qc.transformations]
+    from spinoza_gb300 import _native as nat
+
+    assert names[0] == (nat.H, 0, ()) and names[1] == (nat.H, 1, ())
+    assert names[2] == (nat.X, 2, (1,))
+    assert names[3] == (nat.X, 4, (0, 1))
+    assert names[4][0] == nat.RZ and names[4][1:] == (3, (2,))
+    assert qc.transformations[4].gate.params[0] == pytest.approx(math.pi / 3)
+    assert names[5][0] == nat.SWAP and qc.transformations[5].gate.qubits == (0, 3)
+    assert names[6] == (nat.M, 4, ())
+
+
+@pytest.mark.parametrize("bad", [
+    "qreg q[2]; h q[0];",                       # no header
+    "OPENQASM 2.0; qreg q[2]; foo q[0];",       # unknown gate
+    "OPENQASM 2.0; qreg q[2]; h q[2];",         # index out of range
+    "OPENQASM 2.0; qreg q[2]; rx q[0];",        # missing parameter
+    "OPENQASM 2.0; qreg q[2]; cx q[0];",        # missing argument
+    "OPENQASM 2.0; qreg q[2]; rx(os.system) q[0];",  # not an arithmetic expression
+])
+def test_parse_errors(bad):
+    with pytest.raises(ValueError):
+        openqasm.loads(bad)
+
+
+def test_angle_expressions():
+    assert openqasm.eval_angle("-pi/4") == -math.pi / 4
+    assert openqasm.eval_angle("2*pi - 0.5") == 2 * math.pi - 0.5
+    assert openqasm.eval_angle("(1+2)^2") == 9.0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("src,build", [
+    (IQFT4, lambda qc: qc.iqft([3, 2, 1, 0])),
+    (NONCONTROLLED8, lambda qc: (qc.h(0), qc.x(1), qc.y(2), qc.z(3), qc.rx(1.0, 4), qc.ry(2.0, 5), qc.rz(3.0, 6),
+                                 qc.u(1.0, 2.0, 3.0, 7))),
+])
+def test_loaded_program_executes_like_builder(gpu, src, build):
+    qc = openqasm.loads(src)
+    qc.execute()
+    ref = QuantumCircuit(QuantumRegister(qc.num_qubits))
+    build(ref)
+    ref.execute()
+    a, b = qc.state.to_numpy(), ref.state.to_numpy()
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
