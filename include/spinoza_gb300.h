@@ -60,7 +60,7 @@ enum spz_gate_kind {
   SPZ_GATE_RZ = 8,      /* p[0] = angle                                             */
   SPZ_GATE_SWAP = 9,    /* q0, q1 = the two swapped qubits                          */
   SPZ_GATE_U = 10,      /* p[0..2] = theta, phi, lambda                             */
-  SPZ_GATE_UNITARY = 11,/* dense unitary: not on this path (returns UNSUPPORTED)    */
+  SPZ_GATE_UNITARY = 11,/* dense unitary: applied by spz_apply_unitary, not as an op */
   SPZ_GATE_BITFLIP = 12 /* p[0] = probability, p[1] = uniform draw: X iff p[1] <= p[0] */
 };
 
@@ -206,6 +206,20 @@ typedef struct spz_exec_stats {
  * measured qubit becomes a classical control (circuit.rs:570-578). */
 int spz_circuit_execute(spz_state_t h, const spz_op* ops, size_t nops, spz_tracker* tracker,
                         uint32_t flags, spz_exec_stats* stats);
+
+/* QuantumCircuit::execute on a state held in host memory, the reference's own
+ * setting (`State { reals, imags }`, core.rs:20-42, mutated in place by
+ * circuit.rs:552-600): the input arrays (2^n doubles each, n = the handle's)
+ * are uploaded into the handle, the circuit runs, and the result is written
+ * to the output arrays before the call returns; pass the same arrays for the
+ * reference's in-place behaviour.  For page-locked arrays (cudaHostAlloc /
+ * cudaHostRegister) the upload is cut into 8 slabs that the first tile pass
+ * consumes as they arrive and the download follows the last pass slab by
+ * slab, on a second stream; pageable arrays are copied whole before and
+ * after.  Same flags, tracker and stats as spz_circuit_execute. */
+int spz_circuit_execute_host(spz_state_t h, const double* in_reals, const double* in_imags, double* out_reals,
+                             double* out_imags, const spz_op* ops, size_t nops, spz_tracker* tracker,
+                             uint32_t flags, spz_exec_stats* stats);
 
 /* Plan `ops` for an n-qubit state without running anything (host only; no
  * device is needed): fills the counters spz_circuit_execute would, taking every

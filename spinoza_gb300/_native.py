@@ -130,6 +130,8 @@ SIGNATURES = [
     ("spz_apply_unitary", c_int, [c_void_p, c_void_p, c_void_p, c_uint32, c_uint32, c_int32]),
     ("spz_circuit_execute", c_int, [c_void_p, c_void_p, c_size_t, POINTER(spz_tracker), c_uint32,
                                     POINTER(spz_exec_stats)]),
+    ("spz_circuit_execute_host", c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t,
+                                         POINTER(spz_tracker), c_uint32, POINTER(spz_exec_stats)]),
     ("spz_plan_stats", c_int, [c_uint32, c_void_p, c_size_t, c_uint32, POINTER(spz_exec_stats)]),
     ("spz_plan_schedule", c_int, [c_uint32, c_void_p, c_size_t, c_uint32, c_void_p, c_void_p, c_size_t,
                                   POINTER(c_size_t)]),

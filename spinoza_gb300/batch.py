@@ -106,7 +106,7 @@ class Batch:
             pass
 
 
-CANDIDATES = [(12, 512), (12, 1024), (11, 512), (11, 256), (10, 256), (10, 512)]
+CANDIDATES = [(12, 512), (12, 256), (11, 256), (11, 128), (10, 128), (10, 64)]
 
 
 def _signature(instances: Sequence[Instance]) -> str:

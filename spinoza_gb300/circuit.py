@@ -313,6 +313,38 @@ class QuantumCircuit:
                                                 byref(self.qubit_tracker.c), flags, byref(self.last_stats)))
 
 
+def execute_host(ops: np.ndarray, reals: np.ndarray, imags: np.ndarray, out: Optional[tuple] = None, *,
+                 state: Optional[State] = None, tracker: Optional[QubitTracker] = None, fused: bool = True,
+                 fast: bool = False) -> nat.spz_exec_stats:
+    """QuantumCircuit::execute on a host state (spz_circuit_execute_host): runs
+    `ops` on (reals, imags) and writes the result to `out` = (out_re, out_im),
+    or in place when `out` is None (the reference's behaviour).  Contiguous
+    float64 arrays of 2^n; page-locked arrays (e.g.
+    ``torch.empty(..., pin_memory=True).numpy()``) get copies that overlap the
+    first and last pass.  `state` supplies the device memory (a new n-qubit
+    handle when None)."""
+    out_re, out_im = out if out is not None else (reals, imags)
+    arrs = (reals, imags, out_re, out_im)
+    if any(a.dtype != np.float64 or a.ndim != 1 or a.shape != reals.shape for a in arrs):
+        raise nat.InvalidArgument(nat.SPZ_ERR_INVALID_ARGUMENT, "state arrays must be equal-length float64 vectors")
+    if not all(a.flags.c_contiguous for a in arrs) or not (out_re.flags.writeable and out_im.flags.writeable):
+        raise nat.InvalidArgument(nat.SPZ_ERR_INVALID_ARGUMENT, "state arrays must be contiguous (outputs writeable)")
+    n = int(reals.size).bit_length() - 1
+    if reals.size != 1 << n:
+        raise nat.InvalidArgument(nat.SPZ_ERR_INVALID_ARGUMENT, "the state length must be a power of two")
+    if state is None:
+        state = State(n)
+    elif state.n != n:
+        raise nat.InvalidArgument(nat.SPZ_ERR_INVALID_ARGUMENT, "state size differs from the host arrays")
+    ops = np.ascontiguousarray(ops, dtype=nat.OP_DTYPE)
+    tr = tracker if tracker is not None else QubitTracker()
+    st = nat.spz_exec_stats()
+    nat.check(nat.lib().spz_circuit_execute_host(state.handle, nat.ptr(reals), nat.ptr(imags), nat.ptr(out_re),
+                                                 nat.ptr(out_im), nat.ptr(ops), len(ops), byref(tr.c),
+                                                 _flags(fused, fast), byref(st)))
+    return st
+
+
 def _flags(fused: bool, fast: bool) -> int:
     if fast:
         return nat.EXEC_FAST

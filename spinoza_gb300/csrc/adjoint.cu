@@ -13,11 +13,24 @@
 //
 // Device memory: psi stays in the handle (it holds psi(theta) on return); the
 // sweep runs on two extra state vectors (a working copy of psi, and lam).
+//
+// The backward sweep is fused like the forward executor: the inverse gates,
+// in reverse order, are planned into passes over tiles of 2^k amplitudes that
+// hold psi and lam together in shared memory; per gate and tile each warp adds
+// its share of the gradient to its own accumulator (fixed order: the results
+// are identical from run to run), then the inverse gate is applied to both.
+// Reordering by the planner only exchanges gates that commute, and a gate that
+// commutes with G_j also commutes with its generator K_j (same qubits, same
+// diagonal / non-diagonal roles), so each gradient still sees the states it
+// would see in program order.
 #include <algorithm>
 #include <cstring>
 #include <vector>
 
 #include "common.cuh"
+#include "executor.cuh"
+#include "gate_math.cuh"
+#include "tile_ops.cuh"
 
 namespace spz {
 
@@ -49,45 +62,6 @@ __global__ void adj_finalize_kernel(const double* __restrict__ partials, int nbl
 }
 
 enum GradMode { GM_X = 0, GM_Y = 1, GM_Z = 2, GM_P1 = 3 };
-
-struct GradArgs {
-  const double* pr;  // psi
-  const double* pi;
-  const double* lr;  // lambda
-  const double* li;
-  uint64_t nwork;
-  uint64_t ones;
-  uint64_t tbit;
-  int32_t npos;
-  uint8_t pos[kMaxQubits + 2];
-};
-
-// Im of the per-pair contribution to <lam| Pi sigma |psi> (see file comment).
-template <int MODE>
-__global__ void __launch_bounds__(kAdjThreads) grad_pair_kernel(GradArgs A, double* __restrict__ partials) {
-  __shared__ double smem[32];
-  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  double acc = 0.0;
-  for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < A.nwork; w += stride) {
-    const uint64_t s0 = deposit(w, A.pos, A.npos) | A.ones;
-    const uint64_t s1 = s0 | A.tbit;
-    const double a = A.pr[s0], b = A.pi[s0], c = A.pr[s1], d = A.pi[s1];
-    const double p = A.lr[s0], q = A.li[s0], r = A.lr[s1], s = A.li[s1];
-    double v;
-    if constexpr (MODE == GM_X) {  // Im(conj(l0) psi1 + conj(l1) psi0)
-      v = dadd(dfma(p, d, dmul(dneg(q), c)), dfma(r, b, dmul(dneg(s), a)));
-    } else if constexpr (MODE == GM_Y) {  // Im(-i conj(l0) psi1 + i conj(l1) psi0)
-      v = dsub(dfma(r, a, dmul(s, b)), dfma(p, c, dmul(q, d)));
-    } else if constexpr (MODE == GM_Z) {  // Im(conj(l0) psi0 - conj(l1) psi1)
-      v = dsub(dfma(p, b, dmul(dneg(q), a)), dfma(r, d, dmul(dneg(s), c)));
-    } else {  // Im(conj(l1) psi1)
-      v = dfma(r, d, dmul(dneg(s), c));
-    }
-    acc = dadd(acc, v);
-  }
-  const double t = adj_block_sum(acc, smem);
-  if (threadIdx.x == 0) partials[blockIdx.x] = t;
-}
 
 // lam = D psi for the diagonal terms (or 0 when there are none).
 struct DiagSum {
@@ -147,6 +121,218 @@ __global__ void inner_re_kernel(const double* __restrict__ pr, const double* __r
   if (threadIdx.x == 0) partials[blockIdx.x] = t;
 }
 
+// ------------------------------------------------------------ fused sweep
+#ifndef SPZ_ADJ_TILE_K
+#define SPZ_ADJ_TILE_K 10
+#endif
+#ifndef SPZ_ADJ_THREADS
+#define SPZ_ADJ_THREADS 64
+#endif
+constexpr int kAdjTileK = SPZ_ADJ_TILE_K;  // psi and lam tiles: 4 x 2^10 doubles = 32 KiB
+constexpr int kAdjTileThreads = SPZ_ADJ_THREADS;
+constexpr int kAdjWarps = kAdjTileThreads / 32;
+constexpr int kAdjMaxSlots = 256;   // differentiated gates per backward pass
+
+struct AdjOp {
+  int32_t mode;  // GradMode, or -1: no gradient at this gate
+  int32_t slot;  // its accumulator within the pass
+};
+
+struct AdjPassArgs {
+  double* pr;  // psi (working copy)
+  double* pi;
+  double* lr;  // lam
+  double* li;
+  uint64_t ntiles;
+  const TileGate* gates;  // inverse gates, backward order
+  const AdjOp* aops;
+  double* partials;       // [nslots][gridDim.x]
+  int ngates;
+  int nslots;
+  int k;
+  int c;
+  int nhigh;
+  uint8_t lpos[16];
+};
+
+// Gradient term of one pair / element, as in grad_pair_kernel.
+__device__ __forceinline__ double adj_pair_term(int mode, double a, double b, double c, double d, double p, double q,
+                                                double r, double s) {
+  switch (mode) {
+    case GM_X: return dadd(dfma(p, d, dmul(dneg(q), c)), dfma(r, b, dmul(dneg(s), a)));
+    case GM_Y: return dsub(dfma(r, a, dmul(s, b)), dfma(p, c, dmul(q, d)));
+    case GM_Z: return dsub(dfma(p, b, dmul(dneg(q), a)), dfma(r, d, dmul(dneg(s), c)));
+    default: return dfma(r, d, dmul(dneg(s), c));
+  }
+}
+
+// This thread's gradient share over the gate's pairs, then G^-1 on psi and lam.
+template <int KIND, int NPOS>
+__device__ __forceinline__ double adj_pair(const TileGate& g, int mode, double* pr, double* pi, double* lr, double* li,
+                                           uint32_t nw) {
+  const Enumerator<NPOS, TileGate> E(g);
+  const uint32_t tbit = g.tbit;
+  const Coef cf = g.c;
+  double acc = 0.0;
+  for (uint32_t m = threadIdx.x; m < nw; m += blockDim.x) {
+    const uint32_t s0 = E(m), s1 = s0 | tbit;
+    double a = pr[s0], b = pi[s0], c = pr[s1], d = pi[s1];
+    double p = lr[s0], q = li[s0], r = lr[s1], s = li[s1];
+    if (mode >= 0) acc = dadd(acc, adj_pair_term(mode, a, b, c, d, p, q, r, s));
+    gate_pair<KIND>(cf, a, b, c, d);
+    gate_pair<KIND>(cf, p, q, r, s);
+    pr[s0] = a; pi[s0] = b; pr[s1] = c; pi[s1] = d;
+    lr[s0] = p; li[s0] = q; lr[s1] = r; li[s1] = s;
+  }
+  return acc;
+}
+
+// Diagonal gates (Z, P, RZ): elementwise; the target bit comes from the
+// element or, for a non-local target, from the tile (global_one).  Gradient:
+// Z mode +-Im(conj(lam) psi) by the target bit; P1 mode over the 1 half, which
+// is all the enumeration visits for P.
+template <int KIND, int NPOS>
+__device__ __forceinline__ double adj_diag(const TileGate& g, int mode, int global_one, double* pr, double* pi,
+                                           double* lr, double* li, uint32_t nw) {
+  const Enumerator<NPOS, TileGate> E(g);
+  const uint32_t tbit = g.tbit;
+  const Coef cf = g.c;
+  double acc = 0.0;
+  for (uint32_t m = threadIdx.x; m < nw; m += blockDim.x) {
+    const uint32_t e = E(m);
+    const bool one = global_one >= 0 ? global_one != 0 : (e & tbit) != 0;
+    double a = pr[e], b = pi[e], p = lr[e], q = li[e];
+    if (mode >= 0) {
+      const double v = dfma(p, b, dmul(dneg(q), a));  // Im(conj(lam) psi)
+      acc = (mode == GM_Z && one) ? dsub(acc, v) : dadd(acc, v);
+    }
+    gate_diag<KIND>(cf, one, a, b);
+    gate_diag<KIND>(cf, one, p, q);
+    pr[e] = a; pi[e] = b; lr[e] = p; li[e] = q;
+  }
+  return acc;
+}
+
+template <int KIND>
+__device__ __forceinline__ double adj_pair_any(const TileGate& g, int mode, double* pr, double* pi, double* lr,
+                                               double* li, uint32_t nw) {
+  double r = 0.0;
+#define SPZ_CALL(N) r = adj_pair<KIND, N>(g, mode, pr, pi, lr, li, nw)
+  SPZ_BY_NPOS(g.npos, SPZ_CALL)
+#undef SPZ_CALL
+  return r;
+}
+
+template <int KIND>
+__device__ __forceinline__ double adj_diag_any(const TileGate& g, int mode, int global_one, double* pr, double* pi,
+                                               double* lr, double* li, uint32_t nw) {
+  double r = 0.0;
+#define SPZ_CALL(N) r = adj_diag<KIND, N>(g, mode, global_one, pr, pi, lr, li, nw)
+  SPZ_BY_NPOS(g.npos, SPZ_CALL)
+#undef SPZ_CALL
+  return r;
+}
+
+__global__ void __launch_bounds__(kAdjTileThreads) adj_tile_kernel(AdjPassArgs A) {
+  extern __shared__ double sm[];
+  const int K = A.k;
+  const uint32_t T = 1u << K;
+  double* pr = sm;
+  double* pi = sm + T;
+  double* lr = sm + 2 * T;
+  double* li = sm + 3 * T;
+  uint64_t* rowoff = reinterpret_cast<uint64_t*>(sm + 4 * T);
+  double* wacc = reinterpret_cast<double*>(rowoff + (1u << A.nhigh));  // [kAdjWarps][kAdjMaxSlots]
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t cmask = (1u << A.c) - 1;
+  for (uint32_t r = threadIdx.x; r < (1u << A.nhigh); r += blockDim.x) {
+    uint64_t off = 0;
+    for (int j = 0; j < A.nhigh; ++j)
+      if ((r >> j) & 1) off |= 1ull << A.lpos[A.c + j];
+    rowoff[r] = off;
+  }
+  for (int j = threadIdx.x; j < kAdjWarps * kAdjMaxSlots; j += blockDim.x) wacc[j] = 0.0;
+  __syncthreads();
+  for (uint64_t tile = blockIdx.x; tile < A.ntiles; tile += gridDim.x) {
+    const uint64_t base = deposit(tile, A.lpos, K);
+    for (uint32_t e2 = threadIdx.x; e2 < T / 2; e2 += blockDim.x) {
+      const uint32_t e = 2 * e2;
+      const uint64_t gi = base | rowoff[e >> A.c] | (e & cmask);
+      *reinterpret_cast<double2*>(pr + e) = *reinterpret_cast<const double2*>(A.pr + gi);
+      *reinterpret_cast<double2*>(pi + e) = *reinterpret_cast<const double2*>(A.pi + gi);
+      *reinterpret_cast<double2*>(lr + e) = *reinterpret_cast<const double2*>(A.lr + gi);
+      *reinterpret_cast<double2*>(li + e) = *reinterpret_cast<const double2*>(A.li + gi);
+    }
+    __syncthreads();
+    for (int gi = 0; gi < A.ngates; ++gi) {
+      const TileGate& g = A.gates[gi];
+      if ((base & g.g_ones) != g.g_ones || (base & g.g_zeros) != 0) continue;  // uniform per tile
+      const int mode = A.aops[gi].mode;
+      const uint32_t nw = T >> g.npos;
+      double v = 0.0;
+      switch (g.mode) {
+        case TM_PAIR:
+          switch (g.kind) {
+            case SPZ_GATE_H: v = adj_pair_any<SPZ_GATE_H>(g, mode, pr, pi, lr, li, nw); break;
+            case SPZ_GATE_X: v = adj_pair_any<SPZ_GATE_X>(g, mode, pr, pi, lr, li, nw); break;
+            case SPZ_GATE_Y: v = adj_pair_any<SPZ_GATE_Y>(g, mode, pr, pi, lr, li, nw); break;
+            case SPZ_GATE_RX: v = adj_pair_any<SPZ_GATE_RX>(g, mode, pr, pi, lr, li, nw); break;
+            case SPZ_GATE_RY: v = adj_pair_any<SPZ_GATE_RY>(g, mode, pr, pi, lr, li, nw); break;
+            default: v = adj_pair_any<SPZ_GATE_U>(g, mode, pr, pi, lr, li, nw); break;
+          }
+          break;
+        case TM_DIAG_LOCAL:
+        case TM_DIAG_GLOBAL: {
+          int gone = -1;
+          if (g.mode == TM_DIAG_GLOBAL) {
+            gone = (base & g.g_tbit) ? 1 : 0;
+            if (!gone && g.kind != SPZ_GATE_RZ) break;  // Z / P (and the P1 gradient) live on the 1 half
+          }
+          switch (g.kind) {
+            case SPZ_GATE_Z: v = adj_diag_any<SPZ_GATE_Z>(g, mode, gone, pr, pi, lr, li, nw); break;
+            case SPZ_GATE_P: v = adj_diag_any<SPZ_GATE_P>(g, mode, gone, pr, pi, lr, li, nw); break;
+            default: v = adj_diag_any<SPZ_GATE_RZ>(g, mode, gone, pr, pi, lr, li, nw); break;
+          }
+          break;
+        }
+        default:  // TM_SWAP: no gradient
+          tile_swap_any(g, pr, pi, nw);
+          tile_swap_any(g, lr, li, nw);
+      }
+      if (mode >= 0) {  // uniform: the whole block takes this branch
+        for (int off = 16; off > 0; off >>= 1) v = dadd(v, __shfl_down_sync(0xffffffffu, v, off));
+        if (lane == 0) wacc[warp * kAdjMaxSlots + A.aops[gi].slot] += v;
+      }
+      __syncthreads();
+    }
+    for (uint32_t e2 = threadIdx.x; e2 < T / 2; e2 += blockDim.x) {
+      const uint32_t e = 2 * e2;
+      const uint64_t gi = base | rowoff[e >> A.c] | (e & cmask);
+      *reinterpret_cast<double2*>(A.pr + gi) = *reinterpret_cast<const double2*>(pr + e);
+      *reinterpret_cast<double2*>(A.pi + gi) = *reinterpret_cast<const double2*>(pi + e);
+      *reinterpret_cast<double2*>(A.lr + gi) = *reinterpret_cast<const double2*>(lr + e);
+      *reinterpret_cast<double2*>(A.li + gi) = *reinterpret_cast<const double2*>(li + e);
+    }
+    __syncthreads();
+  }
+  for (int sl = threadIdx.x; sl < A.nslots; sl += blockDim.x) {
+    double t = 0.0;
+    for (int w = 0; w < kAdjWarps; ++w) t = dadd(t, wacc[w * kAdjMaxSlots + sl]);
+    A.partials[(uint64_t)sl * gridDim.x + blockIdx.x] = t;
+  }
+}
+
+// out[slot_op[s]] = sum over blocks of partials[s][.], one block per slot.
+__global__ void adj_slots_kernel(const double* __restrict__ partials, int nblocks, const int32_t* __restrict__ slot_op,
+                                 double* __restrict__ out) {
+  __shared__ double smem[32];
+  const double* row = partials + (uint64_t)blockIdx.x * nblocks;
+  double v = 0.0;
+  for (int b = threadIdx.x; b < nblocks; b += blockDim.x) v = dadd(v, row[b]);
+  v = adj_block_sum(v, smem);
+  if (threadIdx.x == 0) out[slot_op[blockIdx.x]] = v;
+}
+
 namespace {
 
 int ensure_aux(spz_state_t h, int j) {
@@ -181,20 +367,6 @@ spz_gate inverse_gate(const spz_gate& g) {
       break;
   }
   return r;
-}
-
-// The same handle, viewing other device arrays (no ownership).
-spz_state_s view_of(spz_state_t h, double* re, double* im) {
-  spz_state_s v;
-  v.n = h->n;
-  v.N = h->N;
-  v.re = re;
-  v.im = im;
-  v.owns = false;
-  v.own_stream = nullptr;
-  v.stream = h->stream;
-  v.device = h->device;
-  return v;
 }
 
 }  // namespace
@@ -288,47 +460,125 @@ int adjoint_gradient(spz_state_t h, const spz_op* ops, size_t nops, const uint32
     hamiltonian_x_kernel<<<grid_for(h->N), kThreads, 0, h->stream>>>(h->re, h->im, lr, li, h->N, X);
   }
   SPZ_CHECK_LAUNCH("hamiltonian kernels");
-  // Scratch: partials + one slot per op + the energy slot.
+  // Backward: the inverse gates in reverse order, fused into tile passes
+  // (passes with more than kAdjMaxSlots differentiated gates are cut).
+  std::vector<GateApp> bwd;
+  for (size_t ii = nops; ii-- > 0;) {
+    if (skip[ii]) continue;
+    GateApp g = inv[ii];
+    g.src = (int64_t)ii;
+    bwd.push_back(g);
+  }
+  const int k = std::min<int>((int)n, kAdjTileK);
+  const int c = std::min<int>(kTileLowBits, k);
+  std::vector<PlannedPass> passes;
+  for (PlannedPass& P : plan_passes(bwd, n, k, c, /*exact=*/false)) {
+    PlannedPass cur;
+    cur.local = P.local;
+    int slots = 0;
+    for (const GateApp& g : P.gates) {
+      const bool grad = mode_of[g.src] >= 0;
+      if (grad && slots == kAdjMaxSlots) {
+        passes.push_back(cur);
+        cur.gates.clear();
+        slots = 0;
+      }
+      cur.gates.push_back(g);
+      slots += grad;
+    }
+    if (!cur.gates.empty()) passes.push_back(std::move(cur));
+  }
+  std::vector<TileGate> tg;
+  std::vector<AdjOp> ao;
+  std::vector<int32_t> slot_op;
+  std::vector<size_t> gate_off, slot_off;
+  size_t max_slots = 0;
+  for (const PlannedPass& P : passes) {
+    gate_off.push_back(tg.size());
+    slot_off.push_back(slot_op.size());
+    int slots = 0;
+    for (const GateApp& g : P.gates) {
+      tg.push_back(make_tile_gate(g, P.local));
+      AdjOp a{mode_of[g.src], -1};
+      if (a.mode >= 0) {
+        a.slot = slots++;
+        slot_op.push_back((int32_t)(1 + g.src));
+      }
+      ao.push_back(a);
+    }
+    max_slots = std::max<size_t>(max_slots, (size_t)slots);
+  }
+  gate_off.push_back(tg.size());
+  slot_off.push_back(slot_op.size());
+  // Launch shape: one wave of resident blocks.
+  const uint32_t T = 1u << k;
+  const size_t smem = (4 * (size_t)T + (size_t)(1u << (k - c)) + (size_t)kAdjWarps * kAdjMaxSlots) * sizeof(double);
+  static int resident = 0, sms = kNumSMs;
+  if (!resident) {
+    SPZ_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device));
+    const size_t max_smem = (4 * ((size_t)1 << kAdjTileK) + ((size_t)1 << (kAdjTileK - kTileLowBits)) +
+                             (size_t)kAdjWarps * kAdjMaxSlots) * sizeof(double);
+    SPZ_CUDA(cudaFuncSetAttribute(adj_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem));
+    int per_sm = 0;
+    SPZ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, adj_tile_kernel, kAdjTileThreads, max_smem));
+    resident = std::max(1, per_sm);
+  }
+  const uint64_t ntiles = 1ull << (n - k);
+  const int blocks = (int)std::min<uint64_t>(ntiles, (uint64_t)sms * resident);
+  // Scratch: slots (energy + one per op), partials, then the pass descriptors.
+  const size_t nslot_words = (nops + 8 + 31) / 32 * 32;
+  const size_t npart = std::max<size_t>((size_t)kAdjMaxBlocks, max_slots * (size_t)blocks);
+  const size_t desc_off = (nslot_words + npart) * sizeof(double);
+  const size_t tg_bytes = (tg.size() * sizeof(TileGate) + 255) / 256 * 256;
+  const size_t ao_bytes = (ao.size() * sizeof(AdjOp) + 255) / 256 * 256;
+  const size_t so_bytes = slot_op.size() * sizeof(int32_t);
   void* scratch;
-  rc = ensure_dev_scratch(h, (kAdjMaxBlocks + nops + 8) * sizeof(double), &scratch);
+  rc = ensure_dev_scratch(h, desc_off + tg_bytes + ao_bytes + so_bytes + 256, &scratch);
   if (rc) return rc;
-  double* partials = (double*)scratch;
-  double* slots = partials + kAdjMaxBlocks;  // slots[0] = energy, slots[1 + i] = op i
+  double* slots = (double*)scratch;  // slots[0] = energy, slots[1 + i] = op i
+  double* partials = slots + nslot_words;
+  TileGate* d_tg = (TileGate*)((char*)scratch + desc_off);
+  AdjOp* d_ao = (AdjOp*)((char*)d_tg + tg_bytes);
+  int32_t* d_so = (int32_t*)((char*)d_ao + ao_bytes);
+  // From pageable memory: the runtime stages the bytes before returning.
+  if (!tg.empty()) {
+    SPZ_CUDA(cudaMemcpyAsync(d_tg, tg.data(), tg.size() * sizeof(TileGate), cudaMemcpyHostToDevice, h->stream));
+    SPZ_CUDA(cudaMemcpyAsync(d_ao, ao.data(), ao.size() * sizeof(AdjOp), cudaMemcpyHostToDevice, h->stream));
+  }
+  if (!slot_op.empty())
+    SPZ_CUDA(cudaMemcpyAsync(d_so, slot_op.data(), so_bytes, cudaMemcpyHostToDevice, h->stream));
+  SPZ_CUDA(cudaMemsetAsync(slots, 0, (nops + 1) * sizeof(double), h->stream));
   {
-    const int blocks = std::min<int>(grid_for(h->N, kAdjThreads, 8), kAdjMaxBlocks);
-    inner_re_kernel<<<blocks, kAdjThreads, 0, h->stream>>>(h->re, h->im, lr, li, h->N, partials);
-    adj_finalize_kernel<<<1, 1024, 0, h->stream>>>(partials, blocks, slots);
+    const int rb = std::min<int>(grid_for(h->N, kAdjThreads, 8), kAdjMaxBlocks);
+    inner_re_kernel<<<rb, kAdjThreads, 0, h->stream>>>(h->re, h->im, lr, li, h->N, partials);
+    adj_finalize_kernel<<<1, 1024, 0, h->stream>>>(partials, rb, slots);
   }
   // Working copy of psi.
   SPZ_CUDA(cudaMemcpyAsync(wr, h->re, h->N * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
   SPZ_CUDA(cudaMemcpyAsync(wi, h->im, h->N * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
-  spz_state_s psi_v = view_of(h, wr, wi), lam_v = view_of(h, lr, li);
-  for (size_t ii = nops; ii-- > 0;) {
-    if (skip[ii]) continue;
-    if (mode_of[ii] >= 0) {
-      const GateApp& g = fwd[ii];
-      GradArgs A{};
-      A.pr = wr; A.pi = wi; A.lr = lr; A.li = li;
-      A.ones = g.ones;
-      A.tbit = 1ull << g.target;
-      const uint64_t special = g.ones | g.zeros | A.tbit;
-      for (int q = 0; q < 64; ++q)
-        if ((special >> q) & 1) A.pos[A.npos++] = (uint8_t)q;
-      A.nwork = h->N >> A.npos;
-      const int blocks = std::min<int>(grid_for(A.nwork, kAdjThreads, 8), kAdjMaxBlocks);
-      switch (mode_of[ii]) {
-        case GM_X: grad_pair_kernel<GM_X><<<blocks, kAdjThreads, 0, h->stream>>>(A, partials); break;
-        case GM_Y: grad_pair_kernel<GM_Y><<<blocks, kAdjThreads, 0, h->stream>>>(A, partials); break;
-        case GM_Z: grad_pair_kernel<GM_Z><<<blocks, kAdjThreads, 0, h->stream>>>(A, partials); break;
-        default: grad_pair_kernel<GM_P1><<<blocks, kAdjThreads, 0, h->stream>>>(A, partials); break;
-      }
-      adj_finalize_kernel<<<1, 1024, 0, h->stream>>>(partials, blocks, slots + 1 + ii);
-      SPZ_CHECK_LAUNCH("grad_pair_kernel");
+  for (size_t p = 0; p < passes.size(); ++p) {
+    const PlannedPass& P = passes[p];
+    AdjPassArgs A{};
+    A.pr = wr;
+    A.pi = wi;
+    A.lr = lr;
+    A.li = li;
+    A.ntiles = ntiles;
+    A.gates = d_tg + gate_off[p];
+    A.aops = d_ao + gate_off[p];
+    A.partials = partials;
+    A.ngates = (int)(gate_off[p + 1] - gate_off[p]);
+    A.nslots = (int)(slot_off[p + 1] - slot_off[p]);
+    A.k = (int)P.local.size();
+    A.c = c;
+    A.nhigh = A.k - c;
+    for (int j = 0; j < A.k; ++j) A.lpos[j] = (uint8_t)P.local[j];
+    adj_tile_kernel<<<blocks, kAdjTileThreads, smem, h->stream>>>(A);
+    SPZ_CHECK_LAUNCH("adj_tile_kernel");
+    if (A.nslots) {
+      adj_slots_kernel<<<A.nslots, 256, 0, h->stream>>>(partials, blocks, d_so + slot_off[p], slots);
+      SPZ_CHECK_LAUNCH("adj_slots_kernel");
     }
-    rc = launch_gate(&psi_v, inv[ii]);
-    if (rc) return rc;
-    rc = launch_gate(&lam_v, inv[ii]);
-    if (rc) return rc;
   }
   std::vector<double> host(nops + 1);
   SPZ_CUDA(cudaMemcpyAsync(host.data(), slots, (nops + 1) * sizeof(double), cudaMemcpyDeviceToHost, h->stream));

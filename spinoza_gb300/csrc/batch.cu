@@ -25,6 +25,7 @@
 
 #include "common.cuh"
 #include "gate_math.cuh"
+#include "tile_ops.cuh"
 
 namespace spz {
 
@@ -35,7 +36,7 @@ namespace {
 constexpr int kBatchMaxK = 12;
 constexpr int kBatchLowBits = 3;
 constexpr int kMaxPassParams = 256;  // gradient accumulators per backward pass
-constexpr uint64_t kWorkspaceBudget = 24ull << 30;  // HBM for streamed instances' psi and lam
+constexpr uint64_t kWorkspaceBudget = 128ull << 30;  // HBM for streamed instances' psi and lam
 
 enum BPassKind { BP_FWD = 0, BP_HAM = 1, BP_BWD = 2 };
 enum BMode { BM_PAIR = 0, BM_DIAG_LOCAL = 1, BM_DIAG_GLOBAL = 2, BM_SWAP = 3 };
@@ -111,40 +112,18 @@ __device__ __forceinline__ double bsum(double v, double* red) {
   return r;  // thread 0
 }
 
-template <int KIND>
-__device__ __forceinline__ void b_pair(const BGate& g, double* re, double* im, uint32_t nw) {
-  for (uint32_t m = threadIdx.x; m < nw; m += blockDim.x) {
-    const uint32_t s0 = (uint32_t)deposit(m, g.pos, g.npos) | g.l_ones;
-    const uint32_t s1 = s0 | g.tbit;
-    double a = re[s0], b = im[s0], c = re[s1], d = im[s1];
-    gate_pair<KIND>(g.c, a, b, c, d);
-    re[s0] = a; im[s0] = b; re[s1] = c; im[s1] = d;
-  }
-}
-
-template <int KIND>
-__device__ __forceinline__ void b_diag(const BGate& g, double* re, double* im, uint32_t nw, int gone) {
-  for (uint32_t m = threadIdx.x; m < nw; m += blockDim.x) {
-    const uint32_t e = (uint32_t)deposit(m, g.pos, g.npos) | g.l_ones;
-    const bool one = gone >= 0 ? gone != 0 : (e & g.tbit) != 0;
-    double r = re[e], i = im[e];
-    gate_diag<KIND>(g.c, one, r, i);
-    re[e] = r; im[e] = i;
-  }
-}
-
 // Apply one gate to a tile (caller checked the non-local control predicate).
 __device__ void b_apply(const BGate& g, uint64_t base, double* re, double* im, uint32_t T) {
   const uint32_t nw = T >> g.npos;
   switch (g.mode) {
     case BM_PAIR:
       switch (g.kind) {
-        case SPZ_GATE_H: b_pair<SPZ_GATE_H>(g, re, im, nw); break;
-        case SPZ_GATE_X: b_pair<SPZ_GATE_X>(g, re, im, nw); break;
-        case SPZ_GATE_Y: b_pair<SPZ_GATE_Y>(g, re, im, nw); break;
-        case SPZ_GATE_RX: b_pair<SPZ_GATE_RX>(g, re, im, nw); break;
-        case SPZ_GATE_RY: b_pair<SPZ_GATE_RY>(g, re, im, nw); break;
-        default: b_pair<SPZ_GATE_U>(g, re, im, nw); break;
+        case SPZ_GATE_H: tile_pair_any<SPZ_GATE_H>(g, re, im, nw); break;
+        case SPZ_GATE_X: tile_pair_any<SPZ_GATE_X>(g, re, im, nw); break;
+        case SPZ_GATE_Y: tile_pair_any<SPZ_GATE_Y>(g, re, im, nw); break;
+        case SPZ_GATE_RX: tile_pair_any<SPZ_GATE_RX>(g, re, im, nw); break;
+        case SPZ_GATE_RY: tile_pair_any<SPZ_GATE_RY>(g, re, im, nw); break;
+        default: tile_pair_any<SPZ_GATE_U>(g, re, im, nw); break;
       }
       break;
     case BM_DIAG_LOCAL:
@@ -155,20 +134,14 @@ __device__ void b_apply(const BGate& g, uint64_t base, double* re, double* im, u
         if (!gone && g.kind != SPZ_GATE_RZ) break;
       }
       switch (g.kind) {
-        case SPZ_GATE_Z: b_diag<SPZ_GATE_Z>(g, re, im, nw, gone); break;
-        case SPZ_GATE_P: b_diag<SPZ_GATE_P>(g, re, im, nw, gone); break;
-        default: b_diag<SPZ_GATE_RZ>(g, re, im, nw, gone); break;
+        case SPZ_GATE_Z: tile_diag_any<SPZ_GATE_Z>(g, re, im, nw, gone); break;
+        case SPZ_GATE_P: tile_diag_any<SPZ_GATE_P>(g, re, im, nw, gone); break;
+        default: tile_diag_any<SPZ_GATE_RZ>(g, re, im, nw, gone); break;
       }
       break;
     }
     default:
-      for (uint32_t m = threadIdx.x; m < nw; m += blockDim.x) {
-        const uint32_t b0 = (uint32_t)deposit(m, g.pos, g.npos) | g.l_ones;
-        const uint32_t i = b0 | g.tbit2, j = b0 | g.tbit;
-        const double r = re[i], q = im[i];
-        re[i] = re[j]; im[i] = im[j];
-        re[j] = r; im[j] = q;
-      }
+      tile_swap_any(g, re, im, nw);
   }
 }
 
@@ -177,29 +150,32 @@ __device__ void b_apply(const BGate& g, uint64_t base, double* re, double* im, u
 // diagonal generators (Z for RZ, |1><1| for P) are elementwise,
 // sum over x of +-Im(conj(lam_x) psi_x), with the target bit read from the
 // element or, for a non-local target, from the tile base.
-__device__ double b_grad_part(const BGate& g, uint64_t base, const double* pr, const double* pi,
-                              const double* lr, const double* li, uint32_t T) {
-  const uint32_t nw = T >> g.npos;
+template <int NPOS>
+__device__ __forceinline__ double b_grad_part_n(const BGate& g, uint64_t base, const double* pr, const double* pi,
+                                                const double* lr, const double* li, uint32_t nw) {
+  const Enumerator<NPOS, BGate> E(g);
+  const uint32_t tbit = g.tbit;
+  const int grad = g.grad;
   double acc = 0.0;
   if (g.mode != BM_PAIR) {
     const int gone = g.mode == BM_DIAG_GLOBAL ? ((base & g.g_tbit) ? 1 : 0) : -1;
-    if (g.grad == BG_P1 && gone == 0) return 0.0;
+    if (grad == BG_P1 && gone == 0) return 0.0;
     for (uint32_t m = threadIdx.x; m < nw; m += blockDim.x) {
-      const uint32_t e = (uint32_t)deposit(m, g.pos, g.npos) | g.l_ones;
-      const bool one = gone >= 0 ? gone != 0 : (e & g.tbit) != 0;
-      if (g.grad == BG_P1 && !one) continue;
+      const uint32_t e = E(m);
+      const bool one = gone >= 0 ? gone != 0 : (e & tbit) != 0;
+      if (grad == BG_P1 && !one) continue;
       const double v = dfma(lr[e], pi[e], dmul(dneg(li[e]), pr[e]));  // Im(conj(lam) psi)
-      acc = (g.grad == BG_Z && one) ? dsub(acc, v) : dadd(acc, v);
+      acc = (grad == BG_Z && one) ? dsub(acc, v) : dadd(acc, v);
     }
     return acc;
   }
   for (uint32_t m = threadIdx.x; m < nw; m += blockDim.x) {
-    const uint32_t s0 = (uint32_t)deposit(m, g.pos, g.npos) | g.l_ones;
-    const uint32_t s1 = s0 | g.tbit;
+    const uint32_t s0 = E(m);
+    const uint32_t s1 = s0 | tbit;
     const double a = pr[s0], b = pi[s0], c = pr[s1], d = pi[s1];
     const double p = lr[s0], q = li[s0], r = lr[s1], s = li[s1];
     double v;
-    switch (g.grad) {
+    switch (grad) {
       case BG_X: v = dadd(dfma(p, d, dmul(dneg(q), c)), dfma(r, b, dmul(dneg(s), a))); break;
       case BG_Y: v = dsub(dfma(r, a, dmul(s, b)), dfma(p, c, dmul(q, d))); break;
       case BG_Z: v = dsub(dfma(p, b, dmul(dneg(q), a)), dfma(r, d, dmul(dneg(s), c))); break;
@@ -208,6 +184,16 @@ __device__ double b_grad_part(const BGate& g, uint64_t base, const double* pr, c
     acc = dadd(acc, v);
   }
   return acc;
+}
+
+__device__ double b_grad_part(const BGate& g, uint64_t base, const double* pr, const double* pi, const double* lr,
+                              const double* li, uint32_t T) {
+  const uint32_t nw = T >> g.npos;
+  double r = 0.0;
+#define SPZ_CALL(N) r = b_grad_part_n<N>(g, base, pr, pi, lr, li, nw)
+  SPZ_BY_NPOS(g.npos, SPZ_CALL)
+#undef SPZ_CALL
+  return r;
 }
 
 __device__ __forceinline__ uint64_t b_global(uint64_t base, const uint64_t* rowoff, uint32_t e, int c) {
@@ -767,9 +753,13 @@ int build_batch(spz_batch_t b, const spz_batch_instance* inst, size_t ninst, con
   b->grid = std::max(1, std::min<int>(sms * per_sm, (int)ninst));
   if (ws_qubits) {
     // Each CTA owns psi and lam of the largest streamed instance; keep the
-    // workspace within kWorkspaceBudget (at least one CTA per SM).
+    // workspace within half of the free device memory, at most
+    // kWorkspaceBudget (and at least one CTA per SM).
+    size_t free_b = 0, total_b = 0;
+    SPZ_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    const uint64_t budget = std::min<uint64_t>(kWorkspaceBudget, free_b / 2);
     const uint64_t per_cta = 4ull * (1ull << ws_qubits) * sizeof(double);
-    const uint64_t cap = std::max<uint64_t>((uint64_t)sms, kWorkspaceBudget / per_cta);
+    const uint64_t cap = std::max<uint64_t>((uint64_t)sms, budget / per_cta);
     b->grid = (int)std::min<uint64_t>((uint64_t)b->grid, cap);
     const size_t bytes = (size_t)b->grid * 4 * (1ull << ws_qubits) * sizeof(double);
     SPZ_CUDA(cudaMalloc(&b->d_ws, bytes));

@@ -20,6 +20,8 @@
 
 #include "common.cuh"
 #include "gate_math.cuh"
+#include "tile_ops.cuh"
+#include "executor.cuh"
 
 namespace spz {
 
@@ -27,42 +29,10 @@ int measure_qubit(spz_state_t h, uint32_t target, int reset, int forced, double 
                   double* prob0_out);
 int apply_controlled(spz_state_t h, const spz_gate* gate, uint32_t target, uint64_t ones, uint64_t zeros);
 
-constexpr int kTileMaxK = 12;     // 2^12 amplitudes x 16 B = 64 KiB of shared memory
-constexpr int kTileLowBits = 3;   // qubits 0..2 always local: 64-byte contiguous rows
-#ifndef SPZ_TILE_THREADS
-#define SPZ_TILE_THREADS 384  // 3 blocks x 12 warps per SM; 55 registers without spills
-#endif
-#ifndef SPZ_TILE_MIN_BLOCKS
-#define SPZ_TILE_MIN_BLOCKS 3  // 3 x (64 KiB tile + 4 KiB row table) fit one SM's shared memory
-#endif
-constexpr int kTileThreads = SPZ_TILE_THREADS;
-
-enum TileMode { TM_PAIR = 0, TM_DIAG_LOCAL = 1, TM_DIAG_GLOBAL = 2, TM_SWAP = 3, TM_PHASE = 4 };
-
-struct TileGate {
-  int32_t kind;
-  int32_t mode;
-  uint32_t tbit;    // local bit of the target (SWAP: first qubit)
-  uint32_t tbit2;   // SWAP: local bit of the second qubit
-  uint32_t l_ones;  // local bits that must be 1 (controls; plus the target for Z/P on s1)
-  int32_t npos;     // number of local positions inserted by the enumeration
-  uint8_t pos[16];  // sorted local bit positions inserted as zeros
-  uint64_t g_ones;  // non-local bits the tile base must have set
-  uint64_t g_zeros; // non-local bits the tile base must have clear
-  uint64_t g_tbit;  // TM_DIAG_GLOBAL: the non-local target bit
-  Coef c;
-  // TM_PHASE: amplitude x (with x & half_bit, if half_bit != 0) is multiplied by
-  // table[sum_j parity(x & pmask[j]) << j] (complex, ptab .. ptab + 2^pm - 1).
-  uint64_t half_bit;
-  uint64_t pmask[kPhaseMaxTerms];  // parity masks over the global index
-  uint32_t pemask[kPhaseMaxTerms]; // their local part, as bits of the tile offset e
-  int32_t pm;
-  uint32_t ptab;
-};
-
 struct PassArgs {
   double* re;
   double* im;
+  uint64_t tile_begin;  // tiles tile_begin .. ntiles - 1 of the pass
   uint64_t ntiles;
   const TileGate* gates;
   const double2* tables;  // fast-mode phase tables (re, im)
@@ -74,74 +44,64 @@ struct PassArgs {
 };
 
 // ------------------------------------------------------------ device side
-// Every tile op reads its descriptor once, into registers, before its loop:
-// the loop body then touches only shared memory (and, for phase ops, the
-// phase table through L1).
+// Nibble-swizzled tile layout: removes the 2-way bank conflicts of pair ops on
+// tile bits 0-3, but measured no faster on the 30-qubit brickwork (the passes
+// are DFMA-bound, not shared-memory bound), so off by default.
+#ifndef SPZ_TILE_SWIZZLE
+#define SPZ_TILE_SWIZZLE 0
+#endif
+#if SPZ_TILE_SWIZZLE
+using TileSwizzle = NibbleSwizzle;  // tile layout in shared memory (tile_ops.cuh)
+#else
+using TileSwizzle = NoSwizzle;
+#endif
 
-// m -> tile offset with zero bits inserted at the op's sorted local positions
-// (NPOS of them; -1 = any number, read from the descriptor), then l_ones set.
-// Inserting a zero at p is e + (e & ~(2^p - 1)); ascending order keeps the
-// lower insertions in place.
-template <int NPOS>
-struct Enumerator {
-  uint32_t hm[NPOS > 0 ? NPOS : 1];
-  uint32_t ones;
-  __device__ __forceinline__ explicit Enumerator(const TileGate& g) {
-#pragma unroll
-    for (int j = 0; j < NPOS; ++j) hm[j] = ~((1u << g.pos[j]) - 1u);
-    ones = g.l_ones;
-  }
-  __device__ __forceinline__ uint32_t operator()(uint32_t m) const {
-    uint32_t e = m;
-#pragma unroll
-    for (int j = 0; j < NPOS; ++j) e += e & hm[j];
-    return e | ones;
-  }
-};
-
-template <>
-struct Enumerator<-1> {
-  const uint8_t* pos;
-  int npos;
-  uint32_t ones;
-  __device__ __forceinline__ explicit Enumerator(const TileGate& g) : pos(g.pos), npos(g.npos), ones(g.l_ones) {}
-  __device__ __forceinline__ uint32_t operator()(uint32_t m) const {
-    uint32_t e = m;
-    for (int j = 0; j < npos; ++j) e += e & ~((1u << pos[j]) - 1u);
-    return e | ones;
-  }
-};
-
-// Dispatch on the op's insertion count: 0-3 specialised, more generic.
-#define SPZ_BY_NPOS(npos, CALL) \
-  switch (npos) {               \
-    case 0: CALL(0); break;     \
-    case 1: CALL(1); break;     \
-    case 2: CALL(2); break;     \
-    case 3: CALL(3); break;     \
-    default: CALL(-1); break;   \
-  }
-
-template <int KIND, int NPOS>
-__device__ __forceinline__ void tile_pair(const TileGate& g, double* sre, double* sim, uint32_t npairs) {
-  const Enumerator<NPOS> E(g);
+// Lazy op with its phase: s1 *= table[parities], then the lazy rotation.  Lazy
+// ops are uncontrolled, so the target is the only inserted position.  The
+// masks exclude the target, so both members of a pair share the entry.
+template <int FK, int PM>
+__device__ __forceinline__ void tile_fast_phase(const TileGate& g, const double2* __restrict__ tab, uint64_t base,
+                                                double* sre, double* sim, uint32_t npairs) {
+  const Enumerator<1, TileGate> E(g);
   const uint32_t tbit = g.tbit;
   const Coef c = g.c;
+  uint32_t em[PM];
+  uint32_t bidx = 0;
+#pragma unroll
+  for (int j = 0; j < PM; ++j) {
+    bidx |= (uint32_t)(__popcll(base & g.pmask[j]) & 1) << j;
+    em[j] = g.pemask[j];
+  }
+#pragma unroll kTileUnroll
   for (uint32_t m = threadIdx.x; m < npairs; m += blockDim.x) {
-    const uint32_t s0 = E(m);
-    const uint32_t s1 = s0 | tbit;
-    double a = sre[s0], b = sim[s0], x = sre[s1], d = sim[s1];
-    if constexpr (KIND >= FK_LAZY_H) fast_pair<KIND>(c, a, b, x, d);
-    else gate_pair<KIND>(c, a, b, x, d);
+    const uint32_t e0 = E(m);
+    const uint32_t s0 = TileSwizzle::at(e0), s1 = TileSwizzle::at(e0 | tbit);
+    uint32_t idx = bidx;
+#pragma unroll
+    for (int j = 0; j < PM; ++j) idx ^= (uint32_t)(__popc(e0 & em[j]) & 1) << j;
+    const double2 w = __ldg(tab + idx);
+    double a = sre[s0], b = sim[s0];
+    const double r = sre[s1], i = sim[s1];
+    double x = dfma(r, w.x, dmul(dneg(i), w.y));
+    double d = dfma(r, w.y, dmul(i, w.x));
+    fast_pair<FK>(c, a, b, x, d);
     sre[s0] = a; sim[s0] = b; sre[s1] = x; sim[s1] = d;
   }
 }
 
-template <int KIND>
-__device__ __forceinline__ void tile_pair_any(const TileGate& g, double* sre, double* sim, uint32_t npairs) {
-#define SPZ_CALL(N) tile_pair<KIND, N>(g, sre, sim, npairs)
-  SPZ_BY_NPOS(g.npos, SPZ_CALL)
-#undef SPZ_CALL
+template <int FK>
+__device__ __forceinline__ void tile_fast_phase_pm(const TileGate& g, const double2* tab, uint64_t base, double* sre,
+                                                   double* sim, uint32_t npairs) {
+  switch (g.pm) {
+    case 1: tile_fast_phase<FK, 1>(g, tab, base, sre, sim, npairs); break;
+    case 2: tile_fast_phase<FK, 2>(g, tab, base, sre, sim, npairs); break;
+    case 3: tile_fast_phase<FK, 3>(g, tab, base, sre, sim, npairs); break;
+    case 4: tile_fast_phase<FK, 4>(g, tab, base, sre, sim, npairs); break;
+    case 5: tile_fast_phase<FK, 5>(g, tab, base, sre, sim, npairs); break;
+    case 6: tile_fast_phase<FK, 6>(g, tab, base, sre, sim, npairs); break;
+    case 7: tile_fast_phase<FK, 7>(g, tab, base, sre, sim, npairs); break;
+    default: tile_fast_phase<FK, kPhaseMaxTerms>(g, tab, base, sre, sim, npairs); break;
+  }
 }
 
 // Fast-mode phase op: per amplitude, a table entry chosen by index parities.
@@ -152,7 +112,7 @@ __device__ __forceinline__ void tile_pair_any(const TileGate& g, double* sre, do
 template <int NPOS, int PM>
 __device__ __forceinline__ void tile_phase(const TileGate& g, const double2* __restrict__ tab, uint64_t base,
                                            double* sre, double* sim, uint32_t nelem) {
-  const Enumerator<NPOS> E(g);
+  const Enumerator<NPOS, TileGate> E(g);
   uint32_t em[PM > 0 ? PM : 1];
   uint32_t bidx = 0;
 #pragma unroll
@@ -160,11 +120,13 @@ __device__ __forceinline__ void tile_phase(const TileGate& g, const double2* __r
     bidx |= (uint32_t)(__popcll(base & g.pmask[j]) & 1) << j;
     em[j] = g.pemask[j];
   }
+#pragma unroll kTileUnroll
   for (uint32_t m = threadIdx.x; m < nelem; m += blockDim.x) {
-    const uint32_t e = E(m);
+    const uint32_t e0 = E(m);
     uint32_t idx = bidx;
 #pragma unroll
-    for (int j = 0; j < PM; ++j) idx ^= (uint32_t)(__popc(e & em[j]) & 1) << j;
+    for (int j = 0; j < PM; ++j) idx ^= (uint32_t)(__popc(e0 & em[j]) & 1) << j;
+    const uint32_t e = TileSwizzle::at(e0);
     const double2 w = __ldg(tab + idx);
     const double r = sre[e], i = sim[e];
     sre[e] = dfma(r, w.x, dmul(dneg(i), w.y));
@@ -188,41 +150,6 @@ __device__ __forceinline__ void tile_phase_pm(const TileGate& g, const double2* 
   }
 }
 
-template <int KIND, int NPOS>
-__device__ __forceinline__ void tile_diag(const TileGate& g, double* sre, double* sim, uint32_t nelem, int global_one) {
-  const Enumerator<NPOS> E(g);
-  const uint32_t tbit = g.tbit;
-  const Coef c = g.c;
-  for (uint32_t m = threadIdx.x; m < nelem; m += blockDim.x) {
-    const uint32_t e = E(m);
-    const bool one = global_one >= 0 ? global_one != 0 : (e & tbit) != 0;
-    double r = sre[e], i = sim[e];
-    gate_diag<KIND>(c, one, r, i);
-    sre[e] = r; sim[e] = i;
-  }
-}
-
-template <int KIND>
-__device__ __forceinline__ void tile_diag_any(const TileGate& g, double* sre, double* sim, uint32_t nelem,
-                                              int global_one) {
-#define SPZ_CALL(N) tile_diag<KIND, N>(g, sre, sim, nelem, global_one)
-  SPZ_BY_NPOS(g.npos, SPZ_CALL)
-#undef SPZ_CALL
-}
-
-template <int NPOS>
-__device__ __forceinline__ void tile_swap(const TileGate& g, double* sre, double* sim, uint32_t nw) {
-  const Enumerator<NPOS> E(g);
-  const uint32_t t1 = g.tbit, t2 = g.tbit2;
-  for (uint32_t m = threadIdx.x; m < nw; m += blockDim.x) {
-    const uint32_t b0 = E(m);
-    const uint32_t i = b0 | t2, j = b0 | t1;
-    const double r = sre[i], q = sim[i];
-    sre[i] = sre[j]; sim[i] = sim[j];
-    sre[j] = r; sim[j] = q;
-  }
-}
-
 __global__ void __launch_bounds__(kTileThreads, SPZ_TILE_MIN_BLOCKS) tile_kernel(PassArgs A) {
   extern __shared__ double smem[];
   const int K = A.k;
@@ -240,16 +167,23 @@ __global__ void __launch_bounds__(kTileThreads, SPZ_TILE_MIN_BLOCKS) tile_kernel
     rowoff[r] = off;
   }
   __syncthreads();
-  for (uint64_t tile = blockIdx.x; tile < A.ntiles; tile += gridDim.x) {
+  for (uint64_t tile = A.tile_begin + blockIdx.x; tile < A.ntiles; tile += gridDim.x) {
     const uint64_t base = deposit(tile, A.lpos, K);
     // load (pairs of consecutive amplitudes: c >= 1)
     for (uint32_t e2 = threadIdx.x; e2 < T / 2; e2 += blockDim.x) {
       const uint32_t e = 2 * e2;
       const uint64_t gi = base | rowoff[e >> A.c] | (e & cmask);
-      const double2 r = *reinterpret_cast<const double2*>(A.re + gi);
-      const double2 m = *reinterpret_cast<const double2*>(A.im + gi);
-      *reinterpret_cast<double2*>(sre + e) = r;
-      *reinterpret_cast<double2*>(sim + e) = m;
+      double2 r = *reinterpret_cast<const double2*>(A.re + gi);
+      double2 m = *reinterpret_cast<const double2*>(A.im + gi);
+      // e even: e and e + 1 share a 16-byte slot, in reverse order when the
+      // swizzle flips the low bits.
+      const uint32_t p = TileSwizzle::at(e) & ~1u;
+      if (p != e) {
+        r = make_double2(r.y, r.x);
+        m = make_double2(m.y, m.x);
+      }
+      *reinterpret_cast<double2*>(sre + p) = r;
+      *reinterpret_cast<double2*>(sim + p) = m;
     }
     __syncthreads();
     for (int gi = 0; gi < A.ngates; ++gi) {
@@ -259,17 +193,23 @@ __global__ void __launch_bounds__(kTileThreads, SPZ_TILE_MIN_BLOCKS) tile_kernel
       switch (g.mode) {
         case TM_PAIR:
           switch (g.kind) {
-            case SPZ_GATE_H: tile_pair_any<SPZ_GATE_H>(g, sre, sim, nw); break;
-            case SPZ_GATE_X: tile_pair_any<SPZ_GATE_X>(g, sre, sim, nw); break;
-            case SPZ_GATE_Y: tile_pair_any<SPZ_GATE_Y>(g, sre, sim, nw); break;
-            case SPZ_GATE_RX: tile_pair_any<SPZ_GATE_RX>(g, sre, sim, nw); break;
-            case SPZ_GATE_RY: tile_pair_any<SPZ_GATE_RY>(g, sre, sim, nw); break;
-            case FK_LAZY_H: tile_pair_any<FK_LAZY_H>(g, sre, sim, nw); break;
-            case FK_LAZY_RX_A: tile_pair_any<FK_LAZY_RX_A>(g, sre, sim, nw); break;
-            case FK_LAZY_RX_B: tile_pair_any<FK_LAZY_RX_B>(g, sre, sim, nw); break;
-            case FK_LAZY_RY_A: tile_pair_any<FK_LAZY_RY_A>(g, sre, sim, nw); break;
-            case FK_LAZY_RY_B: tile_pair_any<FK_LAZY_RY_B>(g, sre, sim, nw); break;
-            default: tile_pair_any<SPZ_GATE_U>(g, sre, sim, nw); break;
+            case SPZ_GATE_H: tile_pair_any<SPZ_GATE_H, TileGate, TileSwizzle>(g, sre, sim, nw); break;
+            case SPZ_GATE_X: tile_pair_any<SPZ_GATE_X, TileGate, TileSwizzle>(g, sre, sim, nw); break;
+            case SPZ_GATE_Y: tile_pair_any<SPZ_GATE_Y, TileGate, TileSwizzle>(g, sre, sim, nw); break;
+            case SPZ_GATE_RX: tile_pair_any<SPZ_GATE_RX, TileGate, TileSwizzle>(g, sre, sim, nw); break;
+            case SPZ_GATE_RY: tile_pair_any<SPZ_GATE_RY, TileGate, TileSwizzle>(g, sre, sim, nw); break;
+#define SPZ_LAZY(FK)                                                          \
+  case FK:                                                                    \
+    if (g.pm) tile_fast_phase_pm<FK>(g, A.tables + g.ptab, base, sre, sim, nw); \
+    else tile_pair<FK, 1, TileGate, TileSwizzle>(g, sre, sim, nw);            \
+    break;
+            SPZ_LAZY(FK_LAZY_H)
+            SPZ_LAZY(FK_LAZY_RX_A)
+            SPZ_LAZY(FK_LAZY_RX_B)
+            SPZ_LAZY(FK_LAZY_RY_A)
+            SPZ_LAZY(FK_LAZY_RY_B)
+#undef SPZ_LAZY
+            default: tile_pair_any<SPZ_GATE_U, TileGate, TileSwizzle>(g, sre, sim, nw); break;
           }
           break;
         case TM_PHASE:
@@ -284,16 +224,14 @@ __global__ void __launch_bounds__(kTileThreads, SPZ_TILE_MIN_BLOCKS) tile_kernel
             if (!gone && g.kind != SPZ_GATE_RZ) break;  // Z / P act on the 1 half only
           }
           switch (g.kind) {
-            case SPZ_GATE_Z: tile_diag_any<SPZ_GATE_Z>(g, sre, sim, nw, gone); break;
-            case SPZ_GATE_P: tile_diag_any<SPZ_GATE_P>(g, sre, sim, nw, gone); break;
-            default: tile_diag_any<SPZ_GATE_RZ>(g, sre, sim, nw, gone); break;
+            case SPZ_GATE_Z: tile_diag_any<SPZ_GATE_Z, TileGate, TileSwizzle>(g, sre, sim, nw, gone); break;
+            case SPZ_GATE_P: tile_diag_any<SPZ_GATE_P, TileGate, TileSwizzle>(g, sre, sim, nw, gone); break;
+            default: tile_diag_any<SPZ_GATE_RZ, TileGate, TileSwizzle>(g, sre, sim, nw, gone); break;
           }
           break;
         }
         default:  // TM_SWAP
-#define SPZ_CALL(N) tile_swap<N>(g, sre, sim, nw)
-          SPZ_BY_NPOS(g.npos, SPZ_CALL)
-#undef SPZ_CALL
+          tile_swap_any<TileGate, TileSwizzle>(g, sre, sim, nw);
       }
       __syncthreads();
     }
@@ -301,8 +239,15 @@ __global__ void __launch_bounds__(kTileThreads, SPZ_TILE_MIN_BLOCKS) tile_kernel
     for (uint32_t e2 = threadIdx.x; e2 < T / 2; e2 += blockDim.x) {
       const uint32_t e = 2 * e2;
       const uint64_t gi = base | rowoff[e >> A.c] | (e & cmask);
-      *reinterpret_cast<double2*>(A.re + gi) = *reinterpret_cast<const double2*>(sre + e);
-      *reinterpret_cast<double2*>(A.im + gi) = *reinterpret_cast<const double2*>(sim + e);
+      const uint32_t p = TileSwizzle::at(e) & ~1u;
+      double2 r = *reinterpret_cast<const double2*>(sre + p);
+      double2 m = *reinterpret_cast<const double2*>(sim + p);
+      if (p != e) {
+        r = make_double2(r.y, r.x);
+        m = make_double2(m.y, m.x);
+      }
+      *reinterpret_cast<double2*>(A.re + gi) = r;
+      *reinterpret_cast<double2*>(A.im + gi) = m;
     }
     __syncthreads();
   }
@@ -476,6 +421,16 @@ TileGate tile_gate(const GateApp& g, const std::vector<int>& local, const std::v
     t.tbit = 1u << where[g.target];
     special |= t.tbit;
     t.l_ones = l_ones;
+    if (g.kind >= FK_LAZY_H && g.table >= 0) {  // lazy op that first multiplies s1 by a phase entry
+      const PhaseTable& tab = (*tables)[g.table];
+      t.pm = tab.m;
+      for (int j = 0; j < tab.m; ++j) {
+        t.pmask[j] = tab.mask[j];
+        for (int q = 0; q < 64; ++q)
+          if (((tab.mask[j] >> q) & 1) && where[q] >= 0) t.pemask[j] |= 1u << where[q];
+      }
+      t.ptab = (*table_offsets)[g.table];
+    }
   }
   t.npos = 0;
   for (int j = 0; j < 32; ++j)
@@ -485,6 +440,8 @@ TileGate tile_gate(const GateApp& g, const std::vector<int>& local, const std::v
 
 
 }  // namespace
+
+TileGate make_tile_gate(const GateApp& g, const std::vector<int>& local) { return tile_gate(g, local); }
 
 namespace {
 
@@ -544,13 +501,72 @@ bool exactly_commuting_kinds(int a, int b) {
 // FP64-pipe instructions of one executed op (lowered fast ops included).
 uint64_t op_fp64_ops(uint32_t n, const GateApp& g, const std::vector<PhaseTable>& tables) {
   const uint64_t N = 1ull << n;
-  if (g.kind >= FK_LAZY_H && g.kind <= FK_LAZY_RY_B) return 4 * (N / 2);
+  if (g.kind >= FK_LAZY_H && g.kind <= FK_LAZY_RY_B) return (g.table >= 0 ? 8 : 4) * (N / 2);
   if (g.kind == FK_PHASE) return tables[g.table].half_bit ? 4 * (N / 2) : 4 * N;
   return gate_fp64_ops(n, g);
 }
 
-// Run a list of already validated gate applications on h.
-int run_gates(spz_state_t h, const std::vector<GateApp>& gates_in, uint32_t flags, spz_exec_stats* st) {
+// Host arrays that one run of gates uploads from before it and downloads to
+// after it, with the copies overlapping the first and last tile pass where the
+// pass can be cut into kIoChunks slabs: slab j holds the amplitudes whose
+// three slab qubits q, q+1, q+2 read j, where those are the pass's three
+// highest non-local qubits; the pass's tiles then fall into slabs by
+// contiguous ranges of tile index.  In memory a slab is 2^(n-q-3) runs of 2^q
+// amplitudes (one run when q = n-3).
+constexpr int kIoChunks = 8;
+constexpr int kIoMaxRuns = 64;  // copies per slab and array, at most
+struct HostIo {
+  const double* in_re = nullptr;  // upload before the first pass (nullptr: none)
+  const double* in_im = nullptr;
+  double* out_re = nullptr;       // download after the last pass (nullptr: none)
+  double* out_im = nullptr;
+  cudaEvent_t up[kIoChunks] = {};
+  cudaEvent_t down[kIoChunks] = {};
+};
+
+// The lowest slab qubit q for a pass with these local qubits, or -1 when its
+// three highest non-local qubits are not consecutive or a slab would take more
+// than kIoMaxRuns copies.
+int slab_qubit(uint64_t local_mask, uint32_t n) {
+  int top[3], found = 0;
+  for (int q = (int)n - 1; q >= 0 && found < 3; --q)
+    if (!((local_mask >> q) & 1)) top[found++] = q;
+  if (found < 3 || top[1] != top[0] - 1 || top[2] != top[1] - 1) return -1;
+  const int q = top[2];
+  if ((int)n - q - 3 > 6) return -1;
+  return (1 << ((int)n - q - 3)) <= kIoMaxRuns ? q : -1;
+}
+
+// Copy slab j (slab qubits q..q+2) of both arrays on the copy stream.
+int io_copy_slab(spz_state_t h, double* dre, double* dim, const double* sre, const double* sim, int j, int q,
+                 cudaMemcpyKind kind) {
+  const uint64_t runs = 1ull << (h->n - q - 3), len = 1ull << q;
+  for (uint64_t r = 0; r < runs; ++r) {
+    const uint64_t off = (r << (q + 3)) | ((uint64_t)j << q);
+    SPZ_CUDA(cudaMemcpyAsync(dre + off, sre + off, len * sizeof(double), kind, h->copy_stream));
+    SPZ_CUDA(cudaMemcpyAsync(dim + off, sim + off, len * sizeof(double), kind, h->copy_stream));
+  }
+  return SPZ_OK;
+}
+
+// Upload slab j on the copy stream; event up[j] marks it done.
+int io_upload(spz_state_t h, HostIo* io, int j, int q) {
+  int rc = io_copy_slab(h, h->re, h->im, io->in_re, io->in_im, j, q, cudaMemcpyHostToDevice);
+  if (rc) return rc;
+  SPZ_CUDA(cudaEventRecord(io->up[j], h->copy_stream));
+  return SPZ_OK;
+}
+
+// Download slab j on the copy stream once event down[j] (compute) has passed.
+int io_download(spz_state_t h, HostIo* io, int j, int q) {
+  SPZ_CUDA(cudaStreamWaitEvent(h->copy_stream, io->down[j], 0));
+  return io_copy_slab(h, io->out_re, io->out_im, h->re, h->im, j, q, cudaMemcpyDeviceToHost);
+}
+
+// Run a list of already validated gate applications on h (with io: host
+// copies before and after, overlapped where the first / last pass allows).
+int run_gates_io(spz_state_t h, const std::vector<GateApp>& gates_in, uint32_t flags, spz_exec_stats* st,
+                 HostIo* io) {
   if (gates_in.empty()) return SPZ_OK;
   const uint32_t n = h->n;
   const bool fast = (flags & SPZ_EXEC_FAST) != 0;
@@ -563,7 +579,42 @@ int run_gates(spz_state_t h, const std::vector<GateApp>& gates_in, uint32_t flag
   PassTimer timer;
   timer.on = (flags & SPZ_EXEC_TIME_PASSES) != 0;
   timer.stream = h->stream;
+  // Upload slabs in the first tile pass's geometry (or contiguous ones); each
+  // pass waits for what it reads.
+  int up_q = -1;
+  auto queue_uploads = [&](int q) -> int {
+    if (!(io && io->in_re)) return SPZ_OK;
+    up_q = q >= 0 ? q : (int)n - 3;
+    for (int j = 0; j < kIoChunks; ++j) {
+      int rc = io_upload(h, io, j, up_q);
+      if (rc) return rc;
+    }
+    return SPZ_OK;
+  };
+  bool uploaded_wait = false;  // the compute stream already waits for every slab
+  auto wait_all_uploads = [&]() -> int {
+    if (io && io->in_re && !uploaded_wait) {
+      SPZ_CUDA(cudaStreamWaitEvent(h->stream, io->up[kIoChunks - 1], 0));  // slabs upload in order
+      uploaded_wait = true;
+    }
+    return SPZ_OK;
+  };
+  auto download_all = [&]() -> int {
+    if (io && io->out_re) {
+      for (int j = 0; j < kIoChunks; ++j) {
+        SPZ_CUDA(cudaEventRecord(io->down[j], h->stream));
+        int rc = io_download(h, io, j, (int)n - 3);
+        if (rc) return rc;
+      }
+    }
+    return SPZ_OK;
+  };
   if ((flags & SPZ_EXEC_UNFUSED) && !fast) {
+    {
+      int rc = queue_uploads(-1);
+      if (!rc) rc = wait_all_uploads();
+      if (rc) return rc;
+    }
     for (const GateApp& g : gates) {
       int rc = timer.begin();
       if (!rc) rc = launch_gate(h, g);
@@ -576,6 +627,11 @@ int run_gates(spz_state_t h, const std::vector<GateApp>& gates_in, uint32_t flag
         st->passes++;
         st->bytes_moved += gate_algorithmic_bytes(n, g);
       }
+    }
+    int rc = download_all();
+    if (rc) {
+      timer.collect(nullptr);
+      return rc;
     }
     return timer.collect(st);
   }
@@ -633,12 +689,25 @@ int run_gates(spz_state_t h, const std::vector<GateApp>& gates_in, uint32_t flag
     SPZ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tile_kernel, kTileThreads, max_smem));
     resident = std::max(1, per_sm);
   }
+  auto pass_slab_q = [&](const PlannedPass& P) -> int {
+    if (!io || n < 3 || !tiled(P) || (n - P.local.size()) < 3) return -1;
+    uint64_t local_mask = 0;
+    for (int q : P.local) local_mask |= 1ull << q;
+    return slab_qubit(local_mask, n);
+  };
+  {
+    int rc = queue_uploads(passes.empty() ? -1 : pass_slab_q(passes[0]));
+    if (rc) return rc;
+  }
   for (size_t p = 0; p < passes.size(); ++p) {
     const PlannedPass& P = passes[p];
+    const bool last = p + 1 == passes.size();
     if (!tiled(P)) {
-      int rc = timer.begin();
+      int rc = wait_all_uploads();
+      if (!rc) rc = timer.begin();
       if (!rc) rc = launch_gate(h, P.gates[0]);
       if (!rc) rc = timer.end(false);
+      if (!rc && last) rc = download_all();
       if (rc) {
         timer.collect(nullptr);
         return rc;
@@ -663,19 +732,51 @@ int run_gates(spz_state_t h, const std::vector<GateApp>& gates_in, uint32_t flag
     const uint32_t T = 1u << A.k;
     const size_t smem = 2 * T * sizeof(double) + (size_t)(1u << A.nhigh) * sizeof(uint64_t);
     const int threads = (int)std::min<uint32_t>(kTileThreads, std::max<uint32_t>(32, T / 2));
-    const uint64_t blocks = std::min<uint64_t>(A.ntiles, (uint64_t)sms * resident);
-    int rc = timer.begin();
+    // With host copies to overlap, the first / last pass runs slab by slab
+    // (the first pass only in the geometry its uploads were queued in).
+    const int sq = pass_slab_q(P);
+    const bool split_in = sq >= 0 && io->in_re && !uploaded_wait && sq == up_q;
+    const bool split_out = sq >= 0 && io->out_re && last;
+    int rc = SPZ_OK;
+    if (!split_in) rc = wait_all_uploads();
+    if (!rc) rc = timer.begin();
     if (rc) {
       timer.collect(nullptr);
       return rc;
     }
-    tile_kernel<<<(unsigned)blocks, threads, smem, h->stream>>>(A);
-    cudaError_t le = cudaGetLastError();
-    if (le != cudaSuccess) {
-      timer.collect(nullptr);
-      return cuda_fail(le, "tile_kernel");
+    const int launches = (split_in || split_out) ? kIoChunks : 1;
+    const uint64_t per = A.ntiles / launches;
+    for (int j = 0; j < launches; ++j) {
+      PassArgs B = A;
+      B.tile_begin = per * j;
+      B.ntiles = per * (j + 1);
+      if (split_in) {
+        cudaError_t we = cudaStreamWaitEvent(h->stream, io->up[j], 0);
+        if (we != cudaSuccess) {
+          timer.collect(nullptr);
+          return cuda_fail(we, "cudaStreamWaitEvent");
+        }
+      }
+      const uint64_t blocks_j = std::min<uint64_t>(per, (uint64_t)sms * resident);
+      tile_kernel<<<(unsigned)blocks_j, threads, smem, h->stream>>>(B);
+      cudaError_t le = cudaGetLastError();
+      if (le != cudaSuccess) {
+        timer.collect(nullptr);
+        return cuda_fail(le, "tile_kernel");
+      }
+      if (split_out) {
+        cudaError_t re = cudaEventRecord(io->down[j], h->stream);
+        if (re == cudaSuccess) rc = io_download(h, io, j, sq);
+        else rc = cuda_fail(re, "cudaEventRecord");
+        if (rc) {
+          timer.collect(nullptr);
+          return rc;
+        }
+      }
     }
+    if (split_in) uploaded_wait = true;
     rc = timer.end(true);
+    if (!rc && last && !split_out) rc = download_all();
     if (rc) {
       timer.collect(nullptr);
       return rc;
@@ -687,6 +788,11 @@ int run_gates(spz_state_t h, const std::vector<GateApp>& gates_in, uint32_t flag
     }
   }
   return timer.collect(st);
+}
+
+// Run a list of already validated gate applications on h.
+int run_gates(spz_state_t h, const std::vector<GateApp>& gates, uint32_t flags, spz_exec_stats* st) {
+  return run_gates_io(h, gates, flags, st, nullptr);
 }
 
 namespace {
@@ -738,11 +844,36 @@ int op_to_app(spz_state_t h, const spz_op& op, const spz_tracker& tr, bool* skip
 
 }  // namespace
 
+// With io: the state is first uploaded from io's host arrays and finally
+// downloaded to them (the copies overlap the first and last run of gates).
 int execute(spz_state_t h, const spz_op* ops, size_t nops, spz_tracker* tracker, uint32_t flags,
-            spz_exec_stats* st) {
+            spz_exec_stats* st, HostIo* io = nullptr) {
   spz_tracker tr{};
   if (tracker) tr = *tracker;
   std::vector<GateApp> seg;
+  bool in_pending = io && io->in_re;
+  auto run_seg = [&](bool final_seg) -> int {
+    HostIo sub;
+    HostIo* use = nullptr;
+    if (io) {
+      sub = *io;
+      if (!in_pending) sub.in_re = sub.in_im = nullptr;
+      if (!final_seg) sub.out_re = sub.out_im = nullptr;
+      if (sub.in_re || sub.out_re) use = &sub;
+    }
+    in_pending = false;
+    if (!seg.empty()) return run_gates_io(h, seg, flags, st, use);
+    const size_t bytes = h->N * sizeof(double);
+    if (use && use->in_re) {
+      SPZ_CUDA(cudaMemcpyAsync(h->re, use->in_re, bytes, cudaMemcpyHostToDevice, h->stream));
+      SPZ_CUDA(cudaMemcpyAsync(h->im, use->in_im, bytes, cudaMemcpyHostToDevice, h->stream));
+    }
+    if (use && use->out_re) {
+      SPZ_CUDA(cudaMemcpyAsync(use->out_re, h->re, bytes, cudaMemcpyDeviceToHost, h->stream));
+      SPZ_CUDA(cudaMemcpyAsync(use->out_im, h->im, bytes, cudaMemcpyDeviceToHost, h->stream));
+    }
+    return SPZ_OK;
+  };
   for (size_t i = 0; i < nops; ++i) {
     const spz_op& op = ops[i];
     if (op.gate.kind == SPZ_GATE_M) {  // circuit.rs:559-566: a barrier
@@ -750,7 +881,7 @@ int execute(spz_state_t h, const spz_op* ops, size_t nops, spz_tracker* tracker,
         return fail(SPZ_ERR_UNSUPPORTED, "a measurement cannot be controlled");
       if (op.target >= h->n) return fail(SPZ_ERR_INVALID_ARGUMENT, "target qubit out of range");
       if (!((tr.measured >> op.target) & 1)) {
-        int rc = run_gates(h, seg, flags, st);
+        int rc = run_seg(false);
         if (rc) return rc;
         seg.clear();
         uint8_t v = 0;
@@ -773,7 +904,7 @@ int execute(spz_state_t h, const spz_op* ops, size_t nops, spz_tracker* tracker,
       st->algorithmic_bytes += gate_algorithmic_bytes(h->n, a);
     }
   }
-  int rc = run_gates(h, seg, flags, st);
+  int rc = run_seg(true);
   if (rc) return rc;
   if (tracker) *tracker = tr;
   return SPZ_OK;
@@ -866,6 +997,61 @@ int spz_circuit_execute(spz_state_t h, const spz_op* ops, size_t nops, spz_track
   if (nops && !ops) return fail(SPZ_ERR_NULL, "ops is NULL");
   if (stats) std::memset(stats, 0, sizeof(*stats));
   return execute(h, ops, nops, tracker, flags, stats);
+}
+
+int spz_circuit_execute_host(spz_state_t h, const double* in_reals, const double* in_imags, double* out_reals,
+                             double* out_imags, const spz_op* ops, size_t nops, spz_tracker* tracker, uint32_t flags,
+                             spz_exec_stats* stats) {
+  if (!h || !in_reals || !in_imags || !out_reals || !out_imags) return fail(SPZ_ERR_NULL, "NULL argument");
+  if (nops && !ops) return fail(SPZ_ERR_NULL, "ops is NULL");
+  if (stats) std::memset(stats, 0, sizeof(*stats));
+  auto pinned = [](const void* p) {
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    return a.type == cudaMemoryTypeHost;
+  };
+  if (!pinned(in_reals) || !pinned(in_imags) || !pinned(out_reals) || !pinned(out_imags)) {
+    // pageable: staged copies, nothing to overlap
+    int rc = spz_state_upload(h, in_reals, in_imags);
+    if (!rc) rc = execute(h, ops, nops, tracker, flags, stats);
+    if (!rc) rc = spz_state_download(h, out_reals, out_imags);
+    return rc;
+  }
+  if (!h->copy_stream) SPZ_CUDA(cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking));
+  // The copy stream runs every upload slab before any download slab, so the
+  // output may alias the input.
+  HostIo io;
+  io.in_re = in_reals;
+  io.in_im = in_imags;
+  io.out_re = out_reals;
+  io.out_im = out_imags;
+  int rc = SPZ_OK;
+  int made = 0;
+  for (; made < kIoChunks && !rc; ++made) {
+    cudaError_t e1 = cudaEventCreateWithFlags(&io.up[made], cudaEventDisableTiming);
+    cudaError_t e2 = e1 == cudaSuccess ? cudaEventCreateWithFlags(&io.down[made], cudaEventDisableTiming) : e1;
+    if (e1 != cudaSuccess || e2 != cudaSuccess) {
+      if (e1 == cudaSuccess) cudaEventDestroy(io.up[made]);
+      rc = cuda_fail(e1 != cudaSuccess ? e1 : e2, "cudaEventCreateWithFlags");
+      break;
+    }
+  }
+  if (!rc) rc = execute(h, ops, nops, tracker, flags, stats, &io);
+  // Copies may be in flight on either stream (also after an error): they read
+  // and write the caller's arrays, so wait for both before returning.
+  cudaError_t s1 = cudaStreamSynchronize(h->copy_stream);
+  cudaError_t s2 = cudaStreamSynchronize(h->stream);
+  for (int j = 0; j < made; ++j) {
+    cudaEventDestroy(io.up[j]);
+    cudaEventDestroy(io.down[j]);
+  }
+  if (rc) return rc;
+  if (s1 != cudaSuccess) return cuda_fail(s1, "cudaStreamSynchronize");
+  if (s2 != cudaSuccess) return cuda_fail(s2, "cudaStreamSynchronize");
+  return SPZ_OK;
 }
 
 int spz_plan_stats(uint32_t n, const spz_op* ops, size_t nops, uint32_t flags, spz_exec_stats* stats) {

@@ -58,6 +58,9 @@ struct spz_state_s {
   // Two extra state vectors for adjoint differentiation (lazily allocated).
   double* aux_re[2] = {nullptr, nullptr};
   double* aux_im[2] = {nullptr, nullptr};
+  // Second stream for host <-> device copies that overlap tile passes
+  // (spz_circuit_execute_host; lazily created).
+  cudaStream_t copy_stream = nullptr;
 };
 
 namespace spz {

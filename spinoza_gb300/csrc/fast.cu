@@ -17,7 +17,8 @@
 //     Before a gate that acts non-diagonally on qubit q, only the q-dependence
 //     of the pending terms is applied, as one multiply of the q = 1 half by a
 //     small table indexed by the other bits' parities (4 instructions per
-//     pair); the rest stays pending.  At the end (or at a measurement) the
+//     pair; carried by the lazy op itself when one follows); the rest stays
+//     pending.  At the end (or at a measurement) the
 //     remaining terms and G are applied in one table multiply.
 //
 // A brickwork layer of U gates then costs ~8 FP64 instructions per pair and
@@ -80,12 +81,14 @@ struct Lowering {
     out->push_back(g);
   }
 
-  // Apply the q-dependence of the pending terms to the q = 1 half.
-  void flush_half(int q) {
+  // The q-dependence of the pending terms, as tables for the q = 1 half (at
+  // most kPhaseMaxTerms terms each); the q-independent rest stays pending.
+  std::vector<PhaseTable> take_half(int q) {
     const uint64_t qb = 1ull << q;
     std::vector<Term> hit, keep;
     for (const Term& t : terms) ((t.S & qb) ? hit : keep).push_back(t);
     terms.swap(keep);
+    std::vector<PhaseTable> out;
     for (size_t b = 0; b < hit.size(); b += kPhaseMaxTerms) {
       PhaseTable tab;
       tab.half_bit = qb;
@@ -103,9 +106,32 @@ struct Lowering {
         tab.re[idx] = std::cos(ang);
         tab.im[idx] = std::sin(ang);
       }
-      emit_phase(std::move(tab));
+      out.push_back(std::move(tab));
     }
     for (const Term& t : hit) add_term(t.S & ~qb, t.alpha);  // e^{i a p'} stays pending
+    return out;
+  }
+
+  // Apply the q-dependence of the pending terms to the q = 1 half.
+  void flush_half(int q) {
+    for (PhaseTable& tab : take_half(q)) emit_phase(std::move(tab));
+  }
+
+  // A lazy op on q preceded by the q-dependence of the pending terms: the last
+  // (or only) table rides on the lazy op itself (the op multiplies s1 by its
+  // entry before the rotation), the others are separate phase ops.
+  void emit_lazy(int kind, int q, double coef) {
+    std::vector<PhaseTable> tabs = take_half(q);
+    GateApp g = make(kind, (uint32_t)q, coef);
+    if (!tabs.empty()) {
+      for (size_t j = 0; j + 1 < tabs.size(); ++j) emit_phase(std::move(tabs[j]));
+      PhaseTable& last = tabs.back();
+      g.table = (int32_t)tables->size();
+      g.touch = last.half_bit;
+      for (int j = 0; j < last.m; ++j) g.touch |= last.mask[j];
+      tables->push_back(std::move(last));
+    }
+    emit(g);
   }
 
   // Apply every pending term and the global factor.
@@ -192,13 +218,14 @@ struct Lowering {
     return g;
   }
 
-  // RX / RY with cos and sin of theta/2.
+  // RX / RY with cos and sin of theta/2, after the q-dependence of the
+  // pending phases.
   void lazy_rotation(bool is_x, int q, double c, double s) {
     if (std::fabs(c) >= std::fabs(s)) {
-      emit(make(is_x ? FK_LAZY_RX_A : FK_LAZY_RY_A, q, s / c));
+      emit_lazy(is_x ? FK_LAZY_RX_A : FK_LAZY_RY_A, q, s / c);
       scale(c);
     } else {
-      emit(make(is_x ? FK_LAZY_RX_B : FK_LAZY_RY_B, q, c / s));
+      emit_lazy(is_x ? FK_LAZY_RX_B : FK_LAZY_RY_B, q, c / s);
       scale(s);
     }
     renormalise();
@@ -234,14 +261,12 @@ struct Lowering {
           return;
         case SPZ_GATE_SWAP: push_swap((int)g.target, (int)g.target2); emit(g); return;
         case SPZ_GATE_H:
-          flush_half(q);
-          emit(make(FK_LAZY_H, q, 0.0));
+          emit_lazy(FK_LAZY_H, q, 0.0);
           scale(std::sqrt(0.5));
           renormalise();
           return;
         case SPZ_GATE_RX:  // cs = cos(theta/2), sn = sin(theta/2)
         case SPZ_GATE_RY:
-          flush_half(q);
           lazy_rotation(g.kind == SPZ_GATE_RX, q, g.c.cs, g.c.sn);
           return;
         case SPZ_GATE_U: {
@@ -258,7 +283,6 @@ struct Lowering {
             phi = ct < 0.0 ? std::atan2(-g.c.t, -g.c.s) : std::atan2(g.c.t, g.c.s);
           }
           add_term(1ull << q, lambda);
-          flush_half(q);
           lazy_rotation(false, q, ct, st);
           add_term(1ull << q, phi);
           return;

@@ -199,6 +199,10 @@ int spz_state_destroy(spz_state_t h) {
   }
   if (h->dev_scratch.ptr) cudaFree(h->dev_scratch.ptr);
   if (h->host_scratch.ptr) cudaFreeHost(h->host_scratch.ptr);
+  if (h->copy_stream) {
+    cudaStreamSynchronize(h->copy_stream);
+    cudaStreamDestroy(h->copy_stream);
+  }
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
   delete h;
   return SPZ_OK;

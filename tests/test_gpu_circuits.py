@@ -239,3 +239,115 @@ def test_plan_stats_agree_with_execution(gpu):
     planned = circuit.plan_stats(n, ops)
     _, _, st = _run_gpu(n, ops, rng.uniform_state(n, 1))
     assert planned["passes"] == st.passes and planned["bytes_moved"] == st.bytes_moved
+
+
+# ---------------------------------------------------------------- host state
+def _host_pair(init, pinned):
+    """Copies of init as host arrays: page-locked (torch pinned) or pageable."""
+    if not pinned:
+        return init[0].copy(), init[1].copy()
+    import torch
+
+    re = torch.empty(init[0].size, dtype=torch.float64, pin_memory=True).numpy()
+    im = torch.empty(init[1].size, dtype=torch.float64, pin_memory=True).numpy()
+    re[:] = init[0]
+    im[:] = init[1]
+    return re, im
+
+
+def _last_gates_on_top(n):
+    """A last pass with the top qubits local: its slabs are strided runs."""
+    qc = _builder()
+    for q in range(n):
+        qc.ry(0.2 * (q + 1), q)
+    for q in range(n - 1):
+        qc.cx(q, q + 1)
+    qc.h(n - 1)
+    qc.rx(0.3, n - 2)
+    qc.cx(n - 2, n - 1)
+    return qc.ops()
+
+
+def _first_gate_on_top(n):
+    """A first pass whose local qubits include the top qubit (no slabbed upload)."""
+    qc = _builder()
+    qc.h(n - 1)
+    qc.rx(0.7, n - 1)
+    qc.cx(n - 1, 0)
+    for q in range(n):
+        qc.ry(0.1 * (q + 1), q)
+    return qc.ops()
+
+
+@pytest.mark.parametrize("pinned", [True, False], ids=["pinned", "pageable"])
+@pytest.mark.parametrize("case", ["brickwork", "random", "top_first", "top_last", "empty", "unfused"])
+def test_execute_host_equals_device_execute(gpu, pinned, case):
+    """spz_circuit_execute_host (the reference's host State, mutated in place)
+    gives exactly what upload + spz_circuit_execute + download gives."""
+    n = 14
+    init = rng.normal_state(n, 11)
+    fused = case != "unfused"
+    ops = {"brickwork": lambda: brickwork(n, 3), "random": lambda: random_circuit(n, 120, 5),
+           "top_first": lambda: _first_gate_on_top(n), "top_last": lambda: _last_gates_on_top(n),
+           "empty": lambda: np.zeros(0, dtype=nat.OP_DTYPE),
+           "unfused": lambda: brickwork(n, 2)}[case]()
+    want, _, _ = _run_gpu(n, ops, init, fused=fused)
+    re, im = _host_pair(init, pinned)
+    st = circuit.execute_host(ops, re, im, fused=fused)
+    assert np.array_equal(re, want[0]) and np.array_equal(im, want[1])
+    assert st.gates == (len(ops) if case != "empty" else 0)
+
+
+@pytest.mark.parametrize("fast", [False, True], ids=["exact", "fast"])
+def test_execute_host_with_measurements(gpu, fast):
+    """Measurements split the run into segments: the upload feeds the first,
+    the download follows the last, and the tracker comes back."""
+    n = 13
+    init = rng.normal_state(n, 12)
+    qc = _builder()
+    qc.measure(n - 1)       # first segment empty: plain upload before the measurement
+    for q in range(n):
+        qc.u(0.3 + q, 0.2, 0.1 * q, q)
+    qc.measure(3)
+    qc.cx(3, 7)
+    for q in range(n - 1):
+        qc.cx(q, q + 1)
+    ops = qc.ops()
+    ops["gate"]["p"][0, 0] = 0.25
+    ops["gate"]["p"][n + 1, 0] = 0.75
+    s = State.from_arrays(*init)
+    ref = QuantumCircuit.from_state(s, fast=fast)
+    ref.execute_ops(ops)
+    want = s.to_numpy()
+    re, im = _host_pair(init, True)
+    tr = circuit.QubitTracker()
+    circuit.execute_host(ops, re, im, tracker=tr, fast=fast)
+    assert (tr.c.measured, tr.c.values) == (ref.qubit_tracker.c.measured, ref.qubit_tracker.c.values)
+    assert np.array_equal(re, want[0]) and np.array_equal(im, want[1])
+
+
+def test_execute_host_separate_output(gpu):
+    """Input arrays stay untouched when an output pair is given."""
+    n = 15
+    init = rng.normal_state(n, 14)
+    ops = brickwork(n, 2)
+    want, _, _ = _run_gpu(n, ops, init, fused=True)
+    re, im = _host_pair(init, True)
+    ore, oim = _host_pair((np.zeros_like(init[0]), np.zeros_like(init[1])), True)
+    circuit.execute_host(ops, re, im, (ore, oim))
+    assert np.array_equal(re, init[0]) and np.array_equal(im, init[1])
+    assert np.array_equal(ore, want[0]) and np.array_equal(oim, want[1])
+
+
+def test_execute_host_reuses_a_state_and_checks_sizes(gpu):
+    n = 12
+    s = State(n)
+    init = rng.normal_state(n, 13)
+    ops = brickwork(n, 2)
+    for _ in range(2):
+        re, im = _host_pair(init, True)
+        circuit.execute_host(ops, re, im, state=s)
+    want, _, _ = _run_gpu(n, ops, init)
+    assert np.array_equal(re, want[0]) and np.array_equal(im, want[1])
+    with pytest.raises(ValueError):
+        circuit.execute_host(ops, np.zeros(1 << (n + 1)), np.zeros(1 << (n + 1)), state=s)
