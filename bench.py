@@ -136,6 +136,7 @@ def profile_traffic(kernel_file: str):
     if not p.exists():
         return None
     for ln in p.read_text().splitlines():
+        ln = ln.strip()
         if ln.startswith("dram_bytes_per_full_launch:"):
             try:
                 return float(ln.split(":", 1)[1].split()[0])
