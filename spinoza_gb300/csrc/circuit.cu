@@ -36,6 +36,7 @@ struct PassArgs {
   uint64_t ntiles;
   const TileGate* gates;
   const double2* tables;  // fast-mode phase tables (re, im)
+  const int32_t* outcomes;  // device-side measurement outcomes (conditioned gates)
   int ngates;
   int k;            // local qubits
   int c;            // low contiguous local qubits (0..c-1)
@@ -189,6 +190,7 @@ __global__ void __launch_bounds__(kTileThreads, SPZ_TILE_MIN_BLOCKS) tile_kernel
     for (int gi = 0; gi < A.ngates; ++gi) {
       const TileGate& g = A.gates[gi];
       if ((base & g.g_ones) != g.g_ones || (base & g.g_zeros) != 0) continue;  // uniform per tile
+      if (g.cond >= 0 && A.outcomes[g.cond] == 0) continue;                   // classical condition
       const uint32_t nw = T >> g.npos;
       switch (g.mode) {
         case TM_PAIR:
@@ -360,6 +362,7 @@ TileGate tile_gate(const GateApp& g, const std::vector<int>& local, const std::v
   TileGate t{};
   t.kind = g.kind;
   t.c = g.c;
+  t.cond = g.cond;
   if (g.kind == FK_PHASE) {  // elementwise; any qubits (the global index is formed per amplitude)
     const PhaseTable& tab = (*tables)[g.table];
     t.mode = TM_PHASE;
@@ -651,7 +654,7 @@ int run_gates_io(spz_state_t h, const std::vector<GateApp>& gates_in, uint32_t f
   // A pass runs as a tile pass unless it is one exact gate (the plain kernel
   // touches only what that gate needs); lowered fast ops exist only in tiles.
   auto tiled = [&](const PlannedPass& P) {
-    return P.gates.size() > 1 || P.gates[0].kind >= FK_LAZY_H;
+    return P.gates.size() > 1 || P.gates[0].kind >= FK_LAZY_H || P.gates[0].cond >= 0;
   };
   std::vector<TileGate> all;
   std::vector<size_t> offs;
@@ -728,6 +731,7 @@ int run_gates_io(spz_state_t h, const std::vector<GateApp>& gates_in, uint32_t f
     A.ntiles = 1ull << (n - A.k);
     A.gates = dgates + offs[p];
     A.tables = dtables;
+    A.outcomes = h->meas ? reinterpret_cast<const int32_t*>(h->meas + kMeasOutcomeOffset) : nullptr;
     A.ngates = (int)P.gates.size();
     const uint32_t T = 1u << A.k;
     const size_t smem = 2 * T * sizeof(double) + (size_t)(1u << A.nhigh) * sizeof(uint64_t);
@@ -798,10 +802,14 @@ int run_gates(spz_state_t h, const std::vector<GateApp>& gates, uint32_t flags, 
 namespace {
 
 // Resolve one op of a circuit into zero or one GateApp (no M).
-int op_to_app(spz_state_t h, const spz_op& op, const spz_tracker& tr, bool* skip, GateApp* out) {
+// `on_device`: measured qubits whose outcome is only on the device; a Single
+// control on one of them becomes a device-side condition of the gate.
+int op_to_app(spz_state_t h, const spz_op& op, const spz_tracker& tr, uint64_t on_device, bool* skip,
+              GateApp* out) {
   *skip = false;
   spz_gate gate = op.gate;
   uint64_t ones = 0, zeros = 0;
+  int cond = -1;
   switch (op.controls_kind) {
     case SPZ_CONTROLS_NONE:
       break;
@@ -809,7 +817,9 @@ int op_to_app(spz_state_t h, const spz_op& op, const spz_tracker& tr, bool* skip
       if (op.controls == 0 || (op.controls & (op.controls - 1)) != 0)
         return fail(SPZ_ERR_INVALID_ARGUMENT, "Single controls need exactly one control qubit");
       const int c = __builtin_ctzll(op.controls);
-      if ((tr.measured >> c) & 1) {  // classical control (circuit.rs:570-578)
+      if ((on_device >> c) & 1) {  // classical control on a device-side outcome
+        cond = c;
+      } else if ((tr.measured >> c) & 1) {  // classical control (circuit.rs:570-578)
         if (!((tr.values >> c) & 1)) {
           *skip = true;
           return SPZ_OK;
@@ -839,7 +849,9 @@ int op_to_app(spz_state_t h, const spz_op& op, const spz_tracker& tr, bool* skip
     gate = spz_gate{};
     gate.kind = SPZ_GATE_X;
   }
-  return make_gate_app(h->n, gate, op.target, ones, zeros, out);
+  int rc = make_gate_app(h->n, gate, op.target, ones, zeros, out);
+  if (!rc) out->cond = cond;
+  return rc;
 }
 
 }  // namespace
@@ -852,6 +864,10 @@ int execute(spz_state_t h, const spz_op* ops, size_t nops, spz_tracker* tracker,
   if (tracker) tr = *tracker;
   std::vector<GateApp> seg;
   bool in_pending = io && io->in_re;
+  // Measurements stay on the device unless every gate runs as a plain kernel
+  // (which cannot test a device-side condition).
+  const bool device_meas = !(flags & SPZ_EXEC_UNFUSED) || (flags & SPZ_EXEC_FAST);
+  uint64_t on_device = 0;  // qubits measured in this call, outcome on the device
   auto run_seg = [&](bool final_seg) -> int {
     HostIo sub;
     HostIo* use = nullptr;
@@ -884,18 +900,24 @@ int execute(spz_state_t h, const spz_op* ops, size_t nops, spz_tracker* tracker,
         int rc = run_seg(false);
         if (rc) return rc;
         seg.clear();
-        uint8_t v = 0;
-        rc = measure_qubit(h, op.target, 1, -1, op.gate.p[0], &v, nullptr);
-        if (rc) return rc;
+        if (device_meas) {  // outcome stays on the device; later gates test it there
+          rc = measure_on_device(h, op.target, 1, op.gate.p[0]);
+          if (rc) return rc;
+          on_device |= 1ull << op.target;
+        } else {
+          uint8_t v = 0;
+          rc = measure_qubit(h, op.target, 1, -1, op.gate.p[0], &v, nullptr);
+          if (rc) return rc;
+          tr.values = (tr.values & ~(1ull << op.target)) | ((uint64_t)v << op.target);
+        }
         tr.measured |= 1ull << op.target;
-        tr.values = (tr.values & ~(1ull << op.target)) | ((uint64_t)v << op.target);
         if (st) st->passes += 2;
       }
       continue;
     }
     bool skip;
     GateApp a;
-    int rc = op_to_app(h, op, tr, &skip, &a);
+    int rc = op_to_app(h, op, tr, on_device, &skip, &a);
     if (rc) return rc;
     if (skip) continue;
     seg.push_back(a);
@@ -906,6 +928,17 @@ int execute(spz_state_t h, const spz_op* ops, size_t nops, spz_tracker* tracker,
   }
   int rc = run_seg(true);
   if (rc) return rc;
+  if (on_device && tracker) {  // the outcomes measured on the device, into the tracker
+    void* pinned;
+    rc = ensure_host_scratch(h, 64 * sizeof(int32_t), &pinned);
+    if (rc) return rc;
+    SPZ_CUDA(cudaMemcpyAsync(pinned, h->meas + kMeasOutcomeOffset, 64 * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                             h->stream));
+    SPZ_CUDA(cudaStreamSynchronize(h->stream));
+    const int32_t* out = (const int32_t*)pinned;
+    for (int q = 0; q < 64; ++q)
+      if ((on_device >> q) & 1) tr.values = (tr.values & ~(1ull << q)) | ((uint64_t)(out[q] != 0) << q);
+  }
   if (tracker) *tracker = tr;
   return SPZ_OK;
 }
@@ -916,6 +949,8 @@ int plan_stats(uint32_t n, const spz_op* ops, size_t nops, uint32_t flags, spz_e
   spz_state_s fake;
   fake.n = n;
   fake.N = 1ull << n;
+  const bool device_meas = !(flags & SPZ_EXEC_UNFUSED) || (flags & SPZ_EXEC_FAST);
+  uint64_t on_device = 0;
   spz_tracker tr{};
   std::vector<GateApp> seg;
   auto flush = [&]() {
@@ -945,7 +980,7 @@ int plan_stats(uint32_t n, const spz_op* ops, size_t nops, uint32_t flags, spz_e
             pass_of->push_back((uint32_t)st->passes);
           }
         st->passes++;
-        if (P.gates.size() > 1 || P.gates[0].kind >= FK_LAZY_H) {
+        if (P.gates.size() > 1 || P.gates[0].kind >= FK_LAZY_H || P.gates[0].cond >= 0) {
           st->tile_passes++;
           st->bytes_moved += 32ull << n;
         } else {
@@ -962,7 +997,9 @@ int plan_stats(uint32_t n, const spz_op* ops, size_t nops, uint32_t flags, spz_e
       if (op.target >= n) return fail(SPZ_ERR_INVALID_ARGUMENT, "target qubit out of range");
       if (!((tr.measured >> op.target) & 1)) {
         flush();
-        tr.measured |= 1ull << op.target;  // outcome unknown while planning: assume 0
+        tr.measured |= 1ull << op.target;
+        if (device_meas) on_device |= 1ull << op.target;  // later gates: device-side condition
+        // (else the outcome is unknown while planning: assume 0)
         if (order) {
           order->push_back((uint32_t)i);
           pass_of->push_back((uint32_t)st->passes);
@@ -973,7 +1010,7 @@ int plan_stats(uint32_t n, const spz_op* ops, size_t nops, uint32_t flags, spz_e
     }
     bool skip;
     GateApp a;
-    int rc = op_to_app(&fake, op, tr, &skip, &a);
+    int rc = op_to_app(&fake, op, tr, on_device, &skip, &a);
     if (rc) return rc;
     if (skip) continue;
     a.src = (int64_t)i;

@@ -61,6 +61,9 @@ struct spz_state_s {
   // Second stream for host <-> device copies that overlap tile passes
   // (spz_circuit_execute_host; lazily created).
   cudaStream_t copy_stream = nullptr;
+  // Measurements made inside the executor, kept on the device (lazily
+  // allocated): prob0[64], scale[64] (doubles), then outcome[64] (int32).
+  double* meas = nullptr;
 };
 
 namespace spz {
@@ -146,6 +149,7 @@ struct GateApp {
   int64_t src = -1;  // index of the circuit op it came from (planning reports)
   int32_t table = -1;  // FK_PHASE: index of its PhaseTable
   uint64_t touch = 0;  // FK_PHASE: qubits its phases depend on (diagonal action)
+  int32_t cond = -1;   // applies only if the qubit `cond`, measured on the device, read 1
 };
 
 // Fast-mode lowering (fast.cu): rewrite `in` into lazy ops, phase ops and
@@ -181,6 +185,11 @@ std::vector<PlannedPass> plan_passes(const std::vector<GateApp>& gates, uint32_t
 
 // Reductions used by measurement and the executor.
 int prob0_device(spz_state_t h, uint32_t target, double* out);
+// Measure `target` without leaving the device: prob0 -> outcome (1 iff
+// u < 1 - prob0) -> collapse (and reset to 0 when `reset`), the outcome kept in
+// h->meas for gates conditioned on it and for the tracker.
+int measure_on_device(spz_state_t h, uint32_t target, int reset, double u);
+constexpr int kMeasOutcomeOffset = 128;  // doubles before the outcome array in h->meas
 int collapse_device(spz_state_t h, uint32_t target, int outcome, double scale);
 
 }  // namespace spz

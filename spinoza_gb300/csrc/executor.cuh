@@ -47,6 +47,7 @@ struct TileGate {
   uint32_t pemask[kPhaseMaxTerms]; // their local part, as bits of the tile offset e
   int32_t pm;
   uint32_t ptab;
+  int32_t cond;  // >= 0: applies only if that qubit's device-side measurement read 1
 };
 
 // The descriptor of gate g inside a tile pass whose local qubits are `local`

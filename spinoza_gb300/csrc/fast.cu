@@ -234,6 +234,14 @@ struct Lowering {
   void gate(const GateApp& g) {
     const uint64_t controls = g.ones | g.zeros;
     const int q = (int)g.target;
+    if (g.cond >= 0) {  // applied or not by a device-side outcome: stays exact
+      if (!is_diagonal(g.kind)) {  // a diagonal gate commutes with the pending phases
+        flush_half(q);
+        if (g.kind == SPZ_GATE_SWAP) flush_half((int)g.target2);
+      }
+      emit(g);
+      return;
+    }
     if (is_diagonal(g.kind)) {
       if (controls == 0) {
         switch (g.kind) {

@@ -155,6 +155,53 @@ int collapse_device(spz_state_t h, uint32_t target, int outcome, double scale) {
 }
 
 // measure_qubit (measurement.rs:12-92) with an explicit draw.
+// Outcome and scale from prob0 on the device (same arithmetic as measure_qubit).
+__global__ void measure_decide_kernel(double* meas, int t, double u) {
+  const double prob0 = meas[t];
+  const int val = u < 1.0 - prob0 ? 1 : 0;
+  meas[64 + t] = val == 0 ? 1.0 / sqrt(prob0) : 1.0 / sqrt(1.0 - prob0);
+  reinterpret_cast<int32_t*>(meas + kMeasOutcomeOffset)[t] = val;
+}
+
+// Collapse with outcome and scale read from the device; with reset, the kept
+// 1 half lands on the 0 half (collapse followed by X, which only moves).
+__global__ void collapse_meas_kernel(double* __restrict__ re, double* __restrict__ im, uint64_t nwork, int t,
+                                     const double* __restrict__ meas, int reset) {
+  const int outcome = reinterpret_cast<const int32_t*>(meas + kMeasOutcomeOffset)[t];
+  const double scale = meas[64 + t];
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t tbit = 1ull << t, lowmask = tbit - 1;
+  for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < nwork; w += stride) {
+    const uint64_t s0 = ((w & ~lowmask) << 1) | (w & lowmask);
+    const uint64_t s1 = s0 | tbit;
+    const uint64_t keep = outcome ? s1 : s0;
+    const double kr = dmul(re[keep], scale), ki = dmul(im[keep], scale);
+    const bool to0 = !outcome || reset;
+    re[s0] = to0 ? kr : 0.0;
+    im[s0] = to0 ? ki : 0.0;
+    re[s1] = to0 ? 0.0 : kr;
+    im[s1] = to0 ? 0.0 : ki;
+  }
+}
+
+int measure_on_device(spz_state_t h, uint32_t target, int reset, double u) {
+  if (target >= h->n) return fail(SPZ_ERR_INVALID_ARGUMENT, "target qubit out of range");
+  if (!h->meas) {
+    SPZ_CUDA(cudaMalloc(&h->meas, (kMeasOutcomeOffset + 64) * sizeof(double)));
+    SPZ_CUDA(cudaMemsetAsync(h->meas, 0, (kMeasOutcomeOffset + 64) * sizeof(double), h->stream));
+  }
+  void* scratch;
+  int rc = ensure_dev_scratch(h, (kMaxRedBlocks + 8) * sizeof(double), &scratch);
+  if (rc) return rc;
+  rc = pair_reduce_to_device<RED_PROB0>(h, (int)target, (double*)scratch, h->meas + target);
+  if (rc) return rc;
+  measure_decide_kernel<<<1, 1, 0, h->stream>>>(h->meas, (int)target, u);
+  collapse_meas_kernel<<<grid_for(h->N / 2), kThreads, 0, h->stream>>>(h->re, h->im, h->N / 2, (int)target, h->meas,
+                                                                       reset);
+  SPZ_CHECK_LAUNCH("collapse_meas_kernel");
+  return SPZ_OK;
+}
+
 int measure_qubit(spz_state_t h, uint32_t target, int reset, int forced, double u, uint8_t* outcome,
                   double* prob0_out) {
   if (target >= h->n) return fail(SPZ_ERR_INVALID_ARGUMENT, "target qubit out of range");

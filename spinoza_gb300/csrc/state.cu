@@ -203,6 +203,7 @@ int spz_state_destroy(spz_state_t h) {
     cudaStreamSynchronize(h->copy_stream);
     cudaStreamDestroy(h->copy_stream);
   }
+  if (h->meas) cudaFree(h->meas);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
   delete h;
   return SPZ_OK;

@@ -159,6 +159,40 @@ def test_mid_circuit_measurement_and_classical_control(gpu):
         _compare(g, o, exact=False)
 
 
+@pytest.mark.parametrize("mode", ["fused", "fast", "unfused"])
+def test_measurements_on_device_with_conditioned_gates(gpu, mode):
+    """Measurements inside the fused executor stay on the device: the outcome
+    conditions later gates there (a Single control on a measured qubit,
+    circuit.rs:570-578) and reaches the tracker at the end; the unfused mode
+    measures on the host.  Every mode matches the oracle."""
+    n = 11
+    init = rng.normal_state(n, 21)
+    qc = _builder()
+    for q in range(n):
+        qc.ry(0.3 + 0.1 * q, q)
+    qc.measure(4)
+    qc.cx(4, 9)        # conditioned X
+    qc.crz(0.7, 4, 2)  # conditioned diagonal
+    qc.ch(4, 0)        # conditioned pair gate on a low qubit
+    for q in range(n - 1):
+        qc.cx(q, q + 1)
+    qc.measure(9)
+    qc.cry(0.4, 9, 10)
+    qc.u(0.1, 0.2, 0.3, 9)
+    qc.measure(4)      # already measured: no-op
+    ops = qc.ops()
+    m = [i for i in range(len(ops)) if ops["gate"]["kind"][i] == nat.M]
+    for draws in ((0.05, 0.95), (0.95, 0.05), (0.5, 0.5)):
+        ops["gate"]["p"][m[0], 0], ops["gate"]["p"][m[1], 0] = draws
+        s = State.from_arrays(*init)
+        q2 = QuantumCircuit.from_state(s, fused=mode != "unfused", fast=mode == "fast")
+        q2.execute_ops(ops)
+        g = s.to_numpy()
+        o, otr = _run_oracle(ops, init)
+        assert (q2.qubit_tracker.c.measured, q2.qubit_tracker.c.values) == otr
+        _compare(g, o, exact=False)
+
+
 def test_reference_circuit_tests(gpu):
     """circuit.rs:725-822, 962-989, 1030-1061, 1234-1250 restated on the device."""
     # append: H on two one-qubit registers -> 0.5 everywhere
