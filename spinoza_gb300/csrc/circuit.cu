@@ -59,7 +59,9 @@ using TileSwizzle = NoSwizzle;
 
 // Lazy op with its phase: s1 *= table[parities], then the lazy rotation.  Lazy
 // ops are uncontrolled, so the target is the only inserted position.  The
-// masks exclude the target, so both members of a pair share the entry.
+// masks exclude the target, so both members of a pair share the entry.  (The
+// tables, 2-8 entries in a brickwork, are read through L1; holding them one
+// entry per lane and reading them with warp shuffles measured 1.2% slower.)
 template <int FK, int PM>
 __device__ __forceinline__ void tile_fast_phase(const TileGate& g, const double2* __restrict__ tab, uint64_t base,
                                                 double* sre, double* sim, uint32_t npairs) {
