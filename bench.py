@@ -65,6 +65,22 @@ def brickwork_ops(n: int, layers: int, seed: int = 2):
     return ops
 
 
+def replica_throughput(ms_local: float, units_per_replica: float, steps: int, dist=None, device=None):
+    """Replicas only: every rank runs the whole workload on its own GPU, no
+    data-path collective.  Returns (ms, value): the slowest rank's time (max
+    over ranks, the only collective) and the whole job's units per second
+    (units of all ranks / that time)."""
+    import torch
+
+    world = 1
+    if dist is not None:
+        world = dist.get_world_size()
+        t = torch.tensor([ms_local], dtype=torch.float64, device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_local = float(t.item())
+    return ms_local, units_per_replica * world * steps / (ms_local / 1e3)
+
+
 def algorithmic_bytes(ops, n: int) -> int:
     from spinoza_gb300 import circuit
 
@@ -292,13 +308,8 @@ def gpu_arm(args) -> None:
             launches += 1 + st.passes  # reset kernel + one kernel per pass
         e1.record(stream)
         torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms, value = replica_throughput(e0.elapsed_time(e1), abytes / 1e9, args.steps, dist, "cuda")
     ms_step = ms / args.steps
-    value = abytes * world * args.steps / (ms / 1e3) / 1e9
     peaks = measured_peaks()
     N = 1 << n
     tile_avg_ms = tile_ms / max(1, tile_launches)
