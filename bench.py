@@ -527,11 +527,11 @@ def workload_batch(args) -> None:
     from spinoza_gb300.core import State
 
     t0 = time.perf_counter()
-    insts = batch.config5_instances(args.instances)
+    insts = batch.config5_instances(args.instances, qmax=args.batch_qmax)
     t_build = time.perf_counter() - t0
     tune = (batch.autotune(insts, reps=1) if args.autotune
             else {"tile_qubits": args.batch_tile, "threads": args.batch_threads})
-    b = batch.Batch(insts, tile_qubits=tune["tile_qubits"], threads=tune["threads"])
+    b = batch.Batch(insts, tile_qubits=tune["tile_qubits"], threads=tune["threads"], wide_qubits=args.batch_wide)
     b.run()
     t0 = time.perf_counter()
     for _ in range(args.steps):
@@ -553,8 +553,9 @@ def workload_batch(args) -> None:
     nparams = int(b.theta.size)
     _line("config5 batched forward+adjoint instances/s", len(insts) / t_batch, "instances/s", args,
           higher_is_better=True,
-          config={"workload": f"{len(insts)} HEA instances (RY/RZ layers + CZ ring), qubits U{{10..22}}, depth "
-                              f"U{{2..10}}, seeds 8+k", "params": nparams, "launch": tune},
+          config={"workload": f"{len(insts)} HEA instances (RY/RZ layers + CZ ring), qubits U{{10..{args.batch_qmax}}}, depth "
+                              f"U{{2..10}}, seeds 8+k", "params": nparams, "launch": tune,
+                  "wide_qubits": args.batch_wide or 20},
           seconds_per_batch=t_batch, grads_per_s=nparams / t_batch, loop_seconds_extrapolated=t_loop,
           loop_sample=len(sample), speedup_vs_loop=t_loop / t_batch, max_abs_energy_diff=max_e,
           max_abs_grad_diff=max_g, build_seconds=t_build, info=b.info())
@@ -612,6 +613,10 @@ def main() -> None:
     ap.add_argument("--autotune", action="store_true")
     ap.add_argument("--batch-tile", type=int, default=12, help="batch workload: tile qubits (resident up to this n)")
     ap.add_argument("--batch-threads", type=int, default=512, help="batch workload: threads per block")
+    ap.add_argument("--batch-qmax", type=int, default=22, help="batch workload: largest instance (small profiling cases)")
+    ap.add_argument("--batch-wide", type=int, default=0,
+                    help="batch workload: instances of at least this many qubits run across the whole GPU "
+                         "(0: the library default, 31: never)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")

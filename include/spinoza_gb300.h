@@ -328,11 +328,14 @@ typedef struct spz_batch_instance {
 typedef struct spz_batch_config {
   int32_t tile_qubits;    /* local qubits per shared-memory tile, 4..12 (0 = 12) */
   int32_t threads;        /* threads per CTA, multiple of 32 in 64..1024 (0 = 512) */
-  int32_t reserved[2];
+  int32_t wide_qubits;    /* instances of at least this many qubits run one at a time
+                             across the whole GPU (fused passes + fused adjoint sweep)
+                             instead of one per CTA; 0 = 20, > 30 = never            */
+  int32_t reserved;
 } spz_batch_config;
 
 typedef struct spz_batch_stats {
-  uint64_t instances, resident_instances;
+  uint64_t instances, resident_instances;  /* (wide instances count in neither pass total) */
   uint64_t forward_passes, hamiltonian_passes, backward_passes;
   uint64_t ctas, workspace_bytes;
   int32_t tile_qubits, threads;

@@ -84,7 +84,7 @@ class spz_batch_instance(ctypes.Structure):
 
 
 class spz_batch_config(ctypes.Structure):
-    _fields_ = [("tile_qubits", c_int32), ("threads", c_int32), ("reserved", c_int32 * 2)]
+    _fields_ = [("tile_qubits", c_int32), ("threads", c_int32), ("wide_qubits", c_int32), ("reserved", c_int32)]
 
 
 class spz_batch_stats(ctypes.Structure):

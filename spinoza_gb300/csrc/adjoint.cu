@@ -322,6 +322,15 @@ __global__ void __launch_bounds__(kAdjTileThreads) adj_tile_kernel(AdjPassArgs A
   }
 }
 
+// Device outputs: grad[j] = mul[j] * slots[sel[j]], energy = slots[0].
+__global__ void adj_gather_kernel(const double* __restrict__ slots, const int32_t* __restrict__ sel,
+                                  const double* __restrict__ mul, uint32_t nparams, double* __restrict__ grad,
+                                  double* __restrict__ energy) {
+  const uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j < nparams) grad[j] = dmul(mul[j], slots[sel[j]]);
+  if (j == 0) *energy = slots[0];
+}
+
 // out[slot_op[s]] = sum over blocks of partials[s][.], one block per slot.
 __global__ void adj_slots_kernel(const double* __restrict__ partials, int nblocks, const int32_t* __restrict__ slot_op,
                                  double* __restrict__ out) {
@@ -371,12 +380,16 @@ spz_gate inverse_gate(const spz_gate& g) {
 
 }  // namespace
 
+// With d_energy / d_grad (device pointers) the results are written there and
+// nothing waits for the device; otherwise they come back to energy / grad.
 int adjoint_gradient(spz_state_t h, const spz_op* ops, size_t nops, const uint32_t* param_index, size_t nparams,
-                     const spz_pauli_term* terms, size_t nterms, double* energy, double* grad) {
+                     const spz_pauli_term* terms, size_t nterms, double* energy, double* grad, double* d_energy,
+                     double* d_grad) {
+  const bool on_device = d_energy != nullptr;
   if (nops && !ops) return fail(SPZ_ERR_NULL, "ops is NULL");
-  if (nparams && (!param_index || !grad)) return fail(SPZ_ERR_NULL, "param_index/grad is NULL");
+  if (nparams && (!param_index || (on_device ? !d_grad : !grad))) return fail(SPZ_ERR_NULL, "param_index/grad is NULL");
   if (nterms && !terms) return fail(SPZ_ERR_NULL, "terms is NULL");
-  if (!energy) return fail(SPZ_ERR_NULL, "energy is NULL");
+  if (!on_device && !energy) return fail(SPZ_ERR_NULL, "energy is NULL");
   const uint32_t n = h->n;
   // Forward gate list, with each op's inverse.
   std::vector<GateApp> fwd(nops), inv(nops);
@@ -531,22 +544,38 @@ int adjoint_gradient(spz_state_t h, const spz_op* ops, size_t nops, const uint32
   const size_t desc_off = (nslot_words + npart) * sizeof(double);
   const size_t tg_bytes = (tg.size() * sizeof(TileGate) + 255) / 256 * 256;
   const size_t ao_bytes = (ao.size() * sizeof(AdjOp) + 255) / 256 * 256;
-  const size_t so_bytes = slot_op.size() * sizeof(int32_t);
+  const size_t so_bytes = (slot_op.size() * sizeof(int32_t) + 255) / 256 * 256;
+  // device outputs: per parameter, its slot and factor (-2 for P, else 1)
+  std::vector<int32_t> gsel(nparams);
+  std::vector<double> gmul(nparams);
+  for (size_t j = 0; j < nparams; ++j) {
+    gsel[j] = (int32_t)(1 + param_index[j]);
+    gmul[j] = mode_of[param_index[j]] == GM_P1 ? -2.0 : 1.0;
+  }
+  const size_t gs_bytes = (nparams * sizeof(int32_t) + 255) / 256 * 256;
+  const size_t gm_bytes = nparams * sizeof(double);
   void* scratch;
-  rc = ensure_dev_scratch(h, desc_off + tg_bytes + ao_bytes + so_bytes + 256, &scratch);
+  rc = ensure_dev_scratch(h, desc_off + tg_bytes + ao_bytes + so_bytes + gs_bytes + gm_bytes + 256, &scratch);
   if (rc) return rc;
   double* slots = (double*)scratch;  // slots[0] = energy, slots[1 + i] = op i
   double* partials = slots + nslot_words;
   TileGate* d_tg = (TileGate*)((char*)scratch + desc_off);
   AdjOp* d_ao = (AdjOp*)((char*)d_tg + tg_bytes);
   int32_t* d_so = (int32_t*)((char*)d_ao + ao_bytes);
+  int32_t* d_gs = (int32_t*)((char*)d_so + so_bytes);
+  double* d_gm = (double*)((char*)d_gs + gs_bytes);
   // From pageable memory: the runtime stages the bytes before returning.
   if (!tg.empty()) {
     SPZ_CUDA(cudaMemcpyAsync(d_tg, tg.data(), tg.size() * sizeof(TileGate), cudaMemcpyHostToDevice, h->stream));
     SPZ_CUDA(cudaMemcpyAsync(d_ao, ao.data(), ao.size() * sizeof(AdjOp), cudaMemcpyHostToDevice, h->stream));
   }
   if (!slot_op.empty())
-    SPZ_CUDA(cudaMemcpyAsync(d_so, slot_op.data(), so_bytes, cudaMemcpyHostToDevice, h->stream));
+    SPZ_CUDA(cudaMemcpyAsync(d_so, slot_op.data(), slot_op.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
+                             h->stream));
+  if (on_device && nparams) {
+    SPZ_CUDA(cudaMemcpyAsync(d_gs, gsel.data(), nparams * sizeof(int32_t), cudaMemcpyHostToDevice, h->stream));
+    SPZ_CUDA(cudaMemcpyAsync(d_gm, gmul.data(), nparams * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+  }
   SPZ_CUDA(cudaMemsetAsync(slots, 0, (nops + 1) * sizeof(double), h->stream));
   {
     const int rb = std::min<int>(grid_for(h->N, kAdjThreads, 8), kAdjMaxBlocks);
@@ -580,6 +609,12 @@ int adjoint_gradient(spz_state_t h, const spz_op* ops, size_t nops, const uint32
       SPZ_CHECK_LAUNCH("adj_slots_kernel");
     }
   }
+  if (on_device) {
+    adj_gather_kernel<<<(unsigned)std::max<size_t>(1, (nparams + 255) / 256), 256, 0, h->stream>>>(
+        slots, d_gs, d_gm, (uint32_t)nparams, d_grad, d_energy);
+    SPZ_CHECK_LAUNCH("adj_gather_kernel");
+    return SPZ_OK;
+  }
   std::vector<double> host(nops + 1);
   SPZ_CUDA(cudaMemcpyAsync(host.data(), slots, (nops + 1) * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
   SPZ_CUDA(cudaStreamSynchronize(h->stream));
@@ -600,5 +635,5 @@ extern "C" int spz_adjoint_gradient(spz_state_t h, const spz_op* ops, size_t nop
                                     size_t nparams, const spz_pauli_term* terms, size_t nterms, double* energy,
                                     double* grad) {
   if (!h) return fail(SPZ_ERR_NULL, "handle is NULL");
-  return adjoint_gradient(h, ops, nops, param_index, nparams, terms, nterms, energy, grad);
+  return adjoint_gradient(h, ops, nops, param_index, nparams, terms, nterms, energy, grad, nullptr, nullptr);
 }

@@ -37,6 +37,9 @@ constexpr int kBatchMaxK = 12;
 constexpr int kBatchLowBits = 3;
 constexpr int kMaxPassParams = 256;  // gradient accumulators per backward pass
 constexpr uint64_t kWorkspaceBudget = 128ull << 30;  // HBM for streamed instances' psi and lam
+// From 2^20 amplitudes a pass has >= 1024 tiles of 2^10: enough to spread one
+// instance over the GPU; below, one CTA per instance keeps more SMs busy.
+constexpr int kDefaultWideQubits = 20;
 
 enum BPassKind { BP_FWD = 0, BP_HAM = 1, BP_BWD = 2 };
 enum BMode { BM_PAIR = 0, BM_DIAG_LOCAL = 1, BM_DIAG_GLOBAL = 2, BM_SWAP = 3 };
@@ -451,9 +454,23 @@ spz_gate inverse_of(const spz_gate& g) {
 
 }  // namespace
 
+// An instance run across the whole GPU (fused executor + fused adjoint sweep).
+struct WideInst {
+  uint32_t idx = 0, n = 0;
+  std::vector<spz_op> ops;            // angles of parameter ops are set per run
+  std::vector<uint32_t> pidx;         // instance-relative op of each parameter
+  std::vector<spz_pauli_term> terms;
+  uint64_t param_offset = 0;
+  double cost = 0.0;
+};
+
 struct BatchImpl {
   int device = 0;
   int kmax = kBatchMaxK, threads = 512;
+  int wide_qubits = kDefaultWideQubits;
+  uint32_t nnarrow = 0;               // instances in the persistent kernel
+  std::vector<WideInst> wide;         // the others, largest first
+  spz_state_t wide_h[31] = {};        // one state per wide size (lazily created)
   uint32_t ninst = 0;
   uint64_t nparams_total = 0;
   uint32_t ws_qubits = 0;
@@ -492,6 +509,8 @@ namespace {
 void free_batch(spz_batch_t b) {
   if (!b) return;
   if (b->graph) cudaGraphExecDestroy(b->graph);
+  for (spz_state_t w : b->wide_h)
+    if (w) spz_state_destroy(w);
   cudaFree(b->d_inst); cudaFree(b->d_order); cudaFree(b->d_pass); cudaFree(b->d_gates); cudaFree(b->d_terms);
   cudaFree(b->d_jobs); cudaFree(b->d_theta); cudaFree(b->d_energy); cudaFree(b->d_grad); cudaFree(b->d_ws);
   cudaFree(b->d_counter);
@@ -518,10 +537,34 @@ int build_batch(spz_batch_t b, const spz_batch_instance* inst, size_t ninst, con
   std::vector<double> cost(ninst);
   uint64_t ptotal = 0;
   uint32_t ws_qubits = 0;
+  std::vector<uint32_t> narrow;
   for (size_t ii = 0; ii < ninst; ++ii) {
     const spz_batch_instance& in = inst[ii];
     const uint32_t n = in.n;
     if (n == 0 || n > 30) return fail(SPZ_ERR_INVALID_ARGUMENT, "batch instance qubits must be in 1..30");
+    if ((int)n >= b->wide_qubits) {  // whole-GPU path: keep the instance's own lists
+      WideInst w;
+      w.idx = (uint32_t)ii;
+      w.n = n;
+      w.ops.assign(ops + in.op_offset, ops + in.op_offset + in.nops);
+      w.pidx.assign(param_index + in.param_offset, param_index + in.param_offset + in.nparams);
+      w.terms.assign(terms + in.term_offset, terms + in.term_offset + in.nterms);
+      w.param_offset = in.param_offset;
+      w.cost = (double)(in.nops + 8) * (double)(1ull << n);
+      for (uint32_t j = 0; j < in.nparams; ++j) {
+        if (w.pidx[j] >= in.nops) return fail(SPZ_ERR_INVALID_ARGUMENT, "batch param_index out of range");
+        const int kind = w.ops[w.pidx[j]].gate.kind;
+        if (kind != SPZ_GATE_RX && kind != SPZ_GATE_RY && kind != SPZ_GATE_RZ && kind != SPZ_GATE_P)
+          return fail(SPZ_ERR_UNSUPPORTED, "only P, RX, RY and RZ angles can be batch parameters");
+      }
+      for (const spz_op& op : w.ops)
+        if (op.gate.kind == SPZ_GATE_M || op.gate.kind == SPZ_GATE_BITFLIP)
+          return fail(SPZ_ERR_UNSUPPORTED, "measurements and noise cannot be batched");
+      ptotal = std::max<uint64_t>(ptotal, in.param_offset + in.nparams);
+      b->wide.push_back(std::move(w));
+      continue;
+    }
+    narrow.push_back((uint32_t)ii);
     const int k = std::min<int>((int)n, b->kmax);
     const int c = std::min<int>(kBatchLowBits, k);
     // forward gate list (+ which op carries which parameter)
@@ -722,10 +765,11 @@ int build_batch(spz_batch_t b, const spz_batch_instance* inst, size_t ninst, con
     b->resident += I.resident;
     cost[ii] = (double)(applied.size() + 8) * (double)(1ull << n);
   }
-  std::vector<uint32_t> order(ninst);
-  std::iota(order.begin(), order.end(), 0u);
+  std::vector<uint32_t> order = narrow;
   std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t c2) { return cost[a] > cost[c2]; });
+  std::stable_sort(b->wide.begin(), b->wide.end(), [](const WideInst& a, const WideInst& c2) { return a.cost > c2.cost; });
   b->ninst = (uint32_t)ninst;
+  b->nnarrow = (uint32_t)narrow.size();
   b->nparams_total = ptotal;
   b->ws_qubits = ws_qubits;
   b->njobs = (uint32_t)jobs.size();
@@ -750,7 +794,7 @@ int build_batch(spz_batch_t b, const spz_batch_instance* inst, size_t ninst, con
   if (per_sm < 1) return fail(SPZ_ERR_UNSUPPORTED, "batch kernel does not fit on an SM with this configuration");
   int sms = 0;
   SPZ_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device));
-  b->grid = std::max(1, std::min<int>(sms * per_sm, (int)ninst));
+  b->grid = std::max(1, std::min<int>(sms * per_sm, (int)b->nnarrow));
   if (ws_qubits) {
     // Each CTA owns psi and lam of the largest streamed instance; keep the
     // workspace within half of the free device memory, at most
@@ -777,7 +821,7 @@ int capture_graph(spz_batch_t b) {
   BatchArgs A{};
   A.inst = b->d_inst;
   A.order = b->d_order;
-  A.ninst = b->ninst;
+  A.ninst = b->nnarrow;
   A.passes = b->d_pass;
   A.gates = b->d_gates;
   A.terms = b->d_terms;
@@ -787,11 +831,7 @@ int capture_graph(spz_batch_t b) {
   A.ws_qubits = b->ws_qubits;
   A.counter = b->d_counter;
   A.kmax = b->kmax;
-  batch_kernel<<<b->grid, b->threads, b->smem, b->stream>>>(A);
-  cudaMemcpyAsync(b->h_energy, b->d_energy, std::max<size_t>(1, b->ninst) * sizeof(double), cudaMemcpyDeviceToHost,
-                  b->stream);
-  cudaMemcpyAsync(b->h_grad, b->d_grad, std::max<uint64_t>(1, b->nparams_total) * sizeof(double),
-                  cudaMemcpyDeviceToHost, b->stream);
+  if (b->nnarrow) batch_kernel<<<b->grid, b->threads, b->smem, b->stream>>>(A);
   cudaError_t e = cudaStreamEndCapture(b->stream, &g);
   if (e != cudaSuccess) return cuda_fail(e, "batch graph capture");
   e = cudaGraphInstantiate(&b->graph, g, 0);
@@ -816,6 +856,7 @@ int spz_batch_create(const spz_batch_instance* instances, size_t ninstances, con
   if (config) {
     if (config->tile_qubits) b->kmax = config->tile_qubits;
     if (config->threads) b->threads = config->threads;
+    if (config->wide_qubits) b->wide_qubits = config->wide_qubits;
   }
   if (b->kmax < 4 || b->kmax > kBatchMaxK || b->threads < 64 || b->threads > 1024 || (b->threads & 31)) {
     delete b;
@@ -844,6 +885,30 @@ int spz_batch_run(spz_batch_t b, const double* theta, double* energies, double* 
     if (rc) return rc;
   }
   SPZ_CUDA(cudaGraphLaunch(b->graph, b->stream));
+  // Wide instances, largest first, one at a time across the GPU; results
+  // straight into the device output arrays (no wait in between).
+  for (WideInst& w : b->wide) {
+    spz_state_t& h = b->wide_h[w.n];
+    if (!h) {
+      int rc = spz_state_create(w.n, &h);
+      if (rc) return rc;
+      SPZ_CUDA(cudaStreamSynchronize(h->stream));  // its |0...0> fill ran on its own stream
+      h->stream = b->stream;
+    }
+    for (size_t j = 0; j < w.pidx.size(); ++j) w.ops[w.pidx[j]].gate.p[0] = theta[w.param_offset + j];
+    int rc = spz_state_reset_zero(h);
+    if (!rc)
+      rc = adjoint_gradient(h, w.ops.data(), w.ops.size(), w.pidx.data(), w.pidx.size(), w.terms.data(),
+                            w.terms.size(), nullptr, nullptr, b->d_energy + w.idx, b->d_grad + w.param_offset);
+    if (rc) {
+      cudaStreamSynchronize(b->stream);
+      return rc;
+    }
+  }
+  SPZ_CUDA(cudaMemcpyAsync(b->h_energy, b->d_energy, std::max<size_t>(1, b->ninst) * sizeof(double),
+                           cudaMemcpyDeviceToHost, b->stream));
+  SPZ_CUDA(cudaMemcpyAsync(b->h_grad, b->d_grad, std::max<uint64_t>(1, b->nparams_total) * sizeof(double),
+                           cudaMemcpyDeviceToHost, b->stream));
   SPZ_CUDA(cudaStreamSynchronize(b->stream));
   std::memcpy(energies, b->h_energy, b->ninst * sizeof(double));
   if (b->nparams_total) std::memcpy(grads, b->h_grad, b->nparams_total * sizeof(double));

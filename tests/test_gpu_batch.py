@@ -38,6 +38,23 @@ def test_batch_matches_single_instance_adjoint(gpu, tile_qubits, threads):
         assert info["resident_instances"] < len(insts) and info["workspace_bytes"] > 0
 
 
+@pytest.mark.parametrize("wide", [8, 1])
+def test_batch_wide_instances_run_across_the_gpu(gpu, wide):
+    """Instances of at least `wide` qubits take the whole-GPU path (fused
+    executor + fused adjoint sweep, results written on the device); the others
+    stay in the persistent kernel; replays with new angles stay right."""
+    insts = _instances()
+    b = batch.Batch(insts, tile_qubits=6, threads=128, wide_qubits=wide)
+    for shift in (0.0, 0.21):
+        theta = b.theta + shift
+        e, g = b.run(theta)
+        for i, (n, ops, pidx, _, terms) in enumerate(insts):
+            th = b.split(theta)[i]
+            e1, g1 = adjoint.adjoint_gradient(State(n), adjoint.set_params(ops, pidx, th), pidx, terms)
+            assert abs(e[i] - e1) < 1e-12 * max(1.0, abs(e1)), (i, e[i], e1)
+            np.testing.assert_allclose(b.split(g)[i], g1, atol=1e-11, rtol=0)
+
+
 def test_batch_graph_replay_with_new_angles(gpu):
     insts = _instances()[:5]
     b = batch.Batch(insts, tile_qubits=5, threads=128)
