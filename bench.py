@@ -555,7 +555,7 @@ def workload_batch(args) -> None:
           higher_is_better=True,
           config={"workload": f"{len(insts)} HEA instances (RY/RZ layers + CZ ring), qubits U{{10..{args.batch_qmax}}}, depth "
                               f"U{{2..10}}, seeds 8+k", "params": nparams, "launch": tune,
-                  "wide_qubits": args.batch_wide or 20},
+                  "wide_qubits": args.batch_wide or 18},
           seconds_per_batch=t_batch, grads_per_s=nparams / t_batch, loop_seconds_extrapolated=t_loop,
           loop_sample=len(sample), speedup_vs_loop=t_loop / t_batch, max_abs_energy_diff=max_e,
           max_abs_grad_diff=max_g, build_seconds=t_build, info=b.info())

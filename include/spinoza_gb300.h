@@ -330,7 +330,7 @@ typedef struct spz_batch_config {
   int32_t threads;        /* threads per CTA, multiple of 32 in 64..1024 (0 = 512) */
   int32_t wide_qubits;    /* instances of at least this many qubits run one at a time
                              across the whole GPU (fused passes + fused adjoint sweep)
-                             instead of one per CTA; 0 = 20, > 30 = never            */
+                             instead of one per CTA; 0 = 18, > 30 = never            */
   int32_t reserved;
 } spz_batch_config;
 

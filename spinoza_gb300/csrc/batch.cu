@@ -37,9 +37,15 @@ constexpr int kBatchMaxK = 12;
 constexpr int kBatchLowBits = 3;
 constexpr int kMaxPassParams = 256;  // gradient accumulators per backward pass
 constexpr uint64_t kWorkspaceBudget = 128ull << 30;  // HBM for streamed instances' psi and lam
-// From 2^20 amplitudes a pass has >= 1024 tiles of 2^10: enough to spread one
-// instance over the GPU; below, one CTA per instance keeps more SMs busy.
-constexpr int kDefaultWideQubits = 20;
+// From about 2^18 amplitudes one instance (with two more running beside it on
+// other streams) keeps the GPU's block slots busy; below, one CTA per instance
+// does better.  Config 5 (4096 instances of 10-22 qubits) measured 32.5 s with
+// the persistent kernel alone and 26.1-26.7 s with the threshold at 17-20.
+constexpr int kDefaultWideQubits = 18;
+#ifndef SPZ_BATCH_WIDE_STREAMS
+#define SPZ_BATCH_WIDE_STREAMS 3
+#endif
+constexpr int kWideStreams = SPZ_BATCH_WIDE_STREAMS;
 
 enum BPassKind { BP_FWD = 0, BP_HAM = 1, BP_BWD = 2 };
 enum BMode { BM_PAIR = 0, BM_DIAG_LOCAL = 1, BM_DIAG_GLOBAL = 2, BM_SWAP = 3 };
@@ -470,7 +476,12 @@ struct BatchImpl {
   int wide_qubits = kDefaultWideQubits;
   uint32_t nnarrow = 0;               // instances in the persistent kernel
   std::vector<WideInst> wide;         // the others, largest first
-  spz_state_t wide_h[31] = {};        // one state per wide size (lazily created)
+  // Wide instances run on kWideStreams streams at once (a pass of one 20-22
+  // qubit instance leaves block slots empty; another instance fills them),
+  // each stream with its own state per size (lazily created).
+  cudaStream_t wide_stream[kWideStreams] = {};
+  cudaEvent_t wide_done[kWideStreams] = {};
+  spz_state_t wide_h[kWideStreams][31] = {};
   uint32_t ninst = 0;
   uint64_t nparams_total = 0;
   uint32_t ws_qubits = 0;
@@ -509,8 +520,12 @@ namespace {
 void free_batch(spz_batch_t b) {
   if (!b) return;
   if (b->graph) cudaGraphExecDestroy(b->graph);
-  for (spz_state_t w : b->wide_h)
-    if (w) spz_state_destroy(w);
+  for (int si = 0; si < kWideStreams; ++si) {
+    for (spz_state_t w : b->wide_h[si])
+      if (w) spz_state_destroy(w);
+    if (b->wide_done[si]) cudaEventDestroy(b->wide_done[si]);
+    if (b->wide_stream[si]) cudaStreamDestroy(b->wide_stream[si]);
+  }
   cudaFree(b->d_inst); cudaFree(b->d_order); cudaFree(b->d_pass); cudaFree(b->d_gates); cudaFree(b->d_terms);
   cudaFree(b->d_jobs); cudaFree(b->d_theta); cudaFree(b->d_energy); cudaFree(b->d_grad); cudaFree(b->d_ws);
   cudaFree(b->d_counter);
@@ -887,13 +902,27 @@ int spz_batch_run(spz_batch_t b, const double* theta, double* energies, double* 
   SPZ_CUDA(cudaGraphLaunch(b->graph, b->stream));
   // Wide instances, largest first, one at a time across the GPU; results
   // straight into the device output arrays (no wait in between).
-  for (WideInst& w : b->wide) {
-    spz_state_t& h = b->wide_h[w.n];
+  auto wait_all = [&]() {
+    for (int si = 0; si < kWideStreams; ++si)
+      if (b->wide_stream[si]) cudaStreamSynchronize(b->wide_stream[si]);
+    cudaStreamSynchronize(b->stream);
+  };
+  for (size_t wi = 0; wi < b->wide.size(); ++wi) {
+    WideInst& w = b->wide[wi];
+    const int si = (int)(wi % kWideStreams);
+    if (!b->wide_stream[si]) {
+      SPZ_CUDA(cudaStreamCreateWithFlags(&b->wide_stream[si], cudaStreamNonBlocking));
+      SPZ_CUDA(cudaEventCreateWithFlags(&b->wide_done[si], cudaEventDisableTiming));
+    }
+    spz_state_t& h = b->wide_h[si][w.n];
     if (!h) {
       int rc = spz_state_create(w.n, &h);
-      if (rc) return rc;
+      if (rc) {
+        wait_all();
+        return rc;
+      }
       SPZ_CUDA(cudaStreamSynchronize(h->stream));  // its |0...0> fill ran on its own stream
-      h->stream = b->stream;
+      h->stream = b->wide_stream[si];
     }
     for (size_t j = 0; j < w.pidx.size(); ++j) w.ops[w.pidx[j]].gate.p[0] = theta[w.param_offset + j];
     int rc = spz_state_reset_zero(h);
@@ -901,10 +930,15 @@ int spz_batch_run(spz_batch_t b, const double* theta, double* energies, double* 
       rc = adjoint_gradient(h, w.ops.data(), w.ops.size(), w.pidx.data(), w.pidx.size(), w.terms.data(),
                             w.terms.size(), nullptr, nullptr, b->d_energy + w.idx, b->d_grad + w.param_offset);
     if (rc) {
-      cudaStreamSynchronize(b->stream);
+      wait_all();
       return rc;
     }
   }
+  for (int si = 0; si < kWideStreams; ++si)  // the read-back waits for every wide stream
+    if (b->wide_stream[si]) {
+      SPZ_CUDA(cudaEventRecord(b->wide_done[si], b->wide_stream[si]));
+      SPZ_CUDA(cudaStreamWaitEvent(b->stream, b->wide_done[si], 0));
+    }
   SPZ_CUDA(cudaMemcpyAsync(b->h_energy, b->d_energy, std::max<size_t>(1, b->ninst) * sizeof(double),
                            cudaMemcpyDeviceToHost, b->stream));
   SPZ_CUDA(cudaMemcpyAsync(b->h_grad, b->d_grad, std::max<uint64_t>(1, b->nparams_total) * sizeof(double),
