@@ -542,9 +542,17 @@ int slab_qubit(uint64_t local_mask, uint32_t n) {
   return (1 << ((int)n - q - 3)) <= kIoMaxRuns ? q : -1;
 }
 
-// Copy slab j (slab qubits q..q+2) of both arrays on the copy stream.
+// Copy slab j (slab qubits q..q+2) of both arrays on the copy stream.  A state
+// of fewer than 3 qubits (q < 0) is one slab: slab 0 copies it whole.
 int io_copy_slab(spz_state_t h, double* dre, double* dim, const double* sre, const double* sim, int j, int q,
                  cudaMemcpyKind kind) {
+  if (q < 0) {
+    if (j == 0) {
+      SPZ_CUDA(cudaMemcpyAsync(dre, sre, h->N * sizeof(double), kind, h->copy_stream));
+      SPZ_CUDA(cudaMemcpyAsync(dim, sim, h->N * sizeof(double), kind, h->copy_stream));
+    }
+    return SPZ_OK;
+  }
   const uint64_t runs = 1ull << (h->n - q - 3), len = 1ull << q;
   for (uint64_t r = 0; r < runs; ++r) {
     const uint64_t off = (r << (q + 3)) | ((uint64_t)j << q);

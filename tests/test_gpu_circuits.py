@@ -360,6 +360,17 @@ def test_execute_host_with_measurements(gpu, fast):
     assert np.array_equal(re, want[0]) and np.array_equal(im, want[1])
 
 
+@pytest.mark.parametrize("n", [1, 2, 3, 4])
+def test_execute_host_tiny_states(gpu, n):
+    """States smaller than the 8 upload slabs are copied whole."""
+    init = rng.normal_state(n, 30 + n)
+    ops = random_circuit(n, 20, n) if n >= 4 else brickwork(n, 2)
+    want, _, _ = _run_gpu(n, ops, init)
+    re, im = _host_pair(init, True)
+    circuit.execute_host(ops, re, im)
+    assert np.array_equal(re, want[0]) and np.array_equal(im, want[1])
+
+
 def test_execute_host_separate_output(gpu):
     """Input arrays stay untouched when an output pair is given."""
     n = 15
