@@ -583,7 +583,7 @@ def workload_sweep33(args) -> None:
              ("MCX3", lambda t: G.mc_apply(Gate.X, s, [(t + 1) % n, (t + 2) % n, (t + 3) % n], None, t), 4)]
     for name, fn, bpn in kinds:
         for t in range(n):
-            dt = _event_time(lambda: fn(t), 1, 1)
+            dt = _event_time(lambda: fn(t), args.steps, args.warmup)
             gbs = bpn * N / dt / 1e9
             rows.append({"gate": name, "target": t, "ms": dt * 1e3, "gbs": gbs, "frac": gbs / peaks["hbm_gbs"]})
     summary = {}
