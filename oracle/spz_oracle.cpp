@@ -334,26 +334,37 @@ int measure(int n, double* re, double* im, int t, int reset, int forced, double 
 // -------------------------------------------------------------- sampling
 // The library's fixed blocked cumulative order (the reference's reservoir
 // sampler is unseeded, so parity there is defined by this shared rule):
-//   p_i = re*re + im*im; chunks of 256 amplitudes, super-chunks of 1024 chunks;
-//   chunk_total = sequential sum; super_total = sequential sum of its chunk
-//   totals; super_base = exclusive sequential scan; chunk_base = super_base +
-//   exclusive sequential scan of chunk totals inside the super-chunk;
-//   target = u * total (clamped below total); chunk = first c with
-//   chunk_end[c] > target; inside it the running sum r = chunk_base + p_j
-//   (sequential) and the outcome is the first j with r > target, or, if none,
-//   the last j of the chunk with p_j > 0.
-constexpr uint64_t kChunk = 256, kSuper = 1024;
+//   p_i = re*re + im*im; sub-chunks of 32 amplitudes, chunks of 8 sub-chunks
+//   (256 amplitudes), super-chunks of 1024 chunks (all clipped to the state);
+//   sub_total = sequential sum of its p; chunk_total = sequential sum of its
+//   sub_totals; super_total = sequential sum of its chunk totals; super_base =
+//   exclusive sequential scan; chunk_base = super_base + exclusive sequential
+//   scan of chunk totals inside the super-chunk; target = u * total (clamped
+//   below total); chunk = first c with chunk_end[c] > target; inside it the
+//   running sum r = chunk_base + sub_total_k (sequential) picks the first
+//   sub-chunk k with r > target, and from that sub-chunk's base the running
+//   sum r + p_j (sequential) picks the first j with r > target.  When no
+//   sub-chunk (or no j) qualifies, the outcome is the last index with p > 0 in
+//   the chunk (or in the sub-chunk), or the chunk's first index.
+constexpr uint64_t kSub = 32, kChunk = 256, kSuper = 1024;
 
 int sample(int n, const double* re, const double* im, const double* u, uint64_t nshots, uint64_t* out) {
   const uint64_t N = 1ull << n;
   const uint64_t cs = std::min<uint64_t>(N, kChunk);
+  const uint64_t ss = std::min<uint64_t>(cs, kSub);
+  const uint64_t ns = cs / ss;  // sub-chunks per chunk
   const uint64_t nchunks = N / cs;
   const uint64_t nsuper = (nchunks + kSuper - 1) / kSuper;
-  std::vector<double> ct(nchunks), st(nsuper), sb(nsuper), cb(nchunks), ce(nchunks);
+  std::vector<double> sub(N / ss), ct(nchunks), st(nsuper), sb(nsuper), cb(nchunks), ce(nchunks);
   auto prob = [&](uint64_t i) { double r = re[i], m = im[i]; return r * r + m * m; };
+  for (uint64_t b = 0; b < N / ss; ++b) {
+    double t = 0.0;
+    for (uint64_t j = 0; j < ss; ++j) t = t + prob(b * ss + j);
+    sub[b] = t;
+  }
   for (uint64_t c = 0; c < nchunks; ++c) {
     double t = 0.0;
-    for (uint64_t j = 0; j < cs; ++j) t = t + prob(c * cs + j);
+    for (uint64_t k = 0; k < ns; ++k) t = t + sub[c * ns + k];
     ct[c] = t;
   }
   for (uint64_t s = 0; s < nsuper; ++s) {
@@ -384,14 +395,30 @@ int sample(int n, const double* re, const double* im, const double* u, uint64_t 
     }
     const uint64_t c = lo;
     double r = cb[c];
-    uint64_t outcome = UINT64_MAX, last_pos = c * cs;
-    for (uint64_t j = 0; j < cs; ++j) {
-      double pj = prob(c * cs + j);
-      if (pj > 0.0) last_pos = c * cs + j;
-      r = r + pj;
-      if (r > target) { outcome = c * cs + j; break; }
+    uint64_t kk = ns;  // the sub-chunk, ns = none
+    for (uint64_t q = 0; q < ns; ++q) {
+      const double rn = r + sub[c * ns + q];
+      if (rn > target) { kk = q; break; }
+      r = rn;
     }
-    out[k] = outcome == UINT64_MAX ? last_pos : outcome;
+    uint64_t outcome = UINT64_MAX;
+    if (kk < ns) {
+      uint64_t last_pos = UINT64_MAX;
+      for (uint64_t j = 0; j < ss; ++j) {
+        const uint64_t i = c * cs + kk * ss + j;
+        const double pj = prob(i);
+        if (pj > 0.0) last_pos = i;
+        r = r + pj;
+        if (r > target) { outcome = i; break; }
+      }
+      if (outcome == UINT64_MAX) outcome = last_pos;
+    }
+    if (outcome == UINT64_MAX) {  // the last index of the chunk with p > 0, or its first
+      outcome = c * cs;
+      for (uint64_t j = cs; j-- > 0;)
+        if (prob(c * cs + j) > 0.0) { outcome = c * cs + j; break; }
+    }
+    out[k] = outcome;
   }
   return OK;
 }

@@ -638,36 +638,44 @@ int pauli_expectation(spz_state_t h, const spz_pauli_term* terms, size_t nterms,
 
 // ------------------------------------------------------------ sampling
 // Fixed blocked cumulative order (bit-identical to the oracle's restatement):
-// p_i = re*re + im*im; chunks of 256 amplitudes summed sequentially; super-
-// chunks of 1024 chunk totals summed sequentially; exclusive sequential scans
-// for the bases; per shot: target = u * total, first chunk whose end exceeds
-// the target, then a sequential running sum from the chunk's base.
-constexpr uint64_t kChunk = 256, kSuper = 1024;
+// p_i = re*re + im*im; sub-chunks of 32 amplitudes, chunks of 8 sub-chunks,
+// super-chunks of 1024 chunks; every total is a sequential sum of the level
+// below; bases are exclusive sequential scans; per shot: target = u * total,
+// the first chunk whose end exceeds it, then inside the chunk the first
+// sub-chunk whose running end exceeds it, then the first element.  A shot
+// walks at most 8 sub-totals and 32 elements (instead of up to 256 elements).
+constexpr uint64_t kSub = 32, kChunk = 256, kSuper = 1024;
 
 __device__ __forceinline__ double prob_exact(const double* re, const double* im, uint64_t i) {
   const double r = re[i], m = im[i];
   return dadd(dmul(r, r), dmul(m, m));
 }
 
-// One warp sums 32 chunks; chunk data is staged through shared memory so the
-// global loads are coalesced, then each lane folds its chunk in order.
+// One warp covers 32 chunks; data is staged through shared memory 32
+// amplitudes of each chunk at a time (coalesced loads), so each lane folds one
+// sub-chunk per step: its sub-total, then the chunk total from the sub-totals.
 __global__ void __launch_bounds__(128) chunk_total_kernel(const double* __restrict__ re,
                                                           const double* __restrict__ im, uint64_t nchunks,
-                                                          uint64_t cs, double* __restrict__ totals) {
+                                                          uint64_t cs, uint64_t ss, double* __restrict__ totals,
+                                                          double* __restrict__ subs) {
   __shared__ double tile[4][32][33];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint64_t warps_total = (uint64_t)gridDim.x * 4;
+  const uint64_t ns = cs / ss;
   for (uint64_t c0 = ((uint64_t)blockIdx.x * 4 + warp) * 32; c0 < nchunks; c0 += warps_total * 32) {
     double t = 0.0;
-    for (uint64_t j0 = 0; j0 < cs; j0 += 32) {
-      const uint64_t width = cs - j0 < 32 ? cs - j0 : 32;
+    for (uint64_t j0 = 0; j0 < cs; j0 += ss) {
       for (int i = 0; i < 32; ++i) {
         const uint64_t c = c0 + i;
-        if (c < nchunks && (uint64_t)lane < width) tile[warp][i][lane] = prob_exact(re, im, c * cs + j0 + lane);
+        if (c < nchunks && (uint64_t)lane < ss) tile[warp][i][lane] = prob_exact(re, im, c * cs + j0 + lane);
       }
       __syncwarp();
-      if (c0 + lane < nchunks)
-        for (uint64_t j = 0; j < width; ++j) t = dadd(t, tile[warp][lane][j]);
+      if (c0 + lane < nchunks) {
+        double u = 0.0;
+        for (uint64_t j = 0; j < ss; ++j) u = dadd(u, tile[warp][lane][j]);
+        subs[(c0 + lane) * ns + j0 / ss] = u;
+        t = dadd(t, u);
+      }
       __syncwarp();
     }
     if (c0 + lane < nchunks) totals[c0 + lane] = t;
@@ -714,7 +722,8 @@ __global__ void chunk_base_kernel(const double* __restrict__ ct, const double* _
 }
 
 __global__ void sample_kernel(const double* __restrict__ re, const double* __restrict__ im, uint64_t nchunks,
-                              uint64_t cs, const double* __restrict__ cb, const double* __restrict__ ce,
+                              uint64_t cs, uint64_t ss, const double* __restrict__ subs,
+                              const double* __restrict__ cb, const double* __restrict__ ce,
                               const double* __restrict__ total_p, const double* __restrict__ u, uint64_t nshots,
                               uint64_t* __restrict__ out) {
   const uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
@@ -727,33 +736,57 @@ __global__ void sample_kernel(const double* __restrict__ re, const double* __res
     const uint64_t mid = lo + (hi - lo) / 2;
     if (ce[mid] > target) hi = mid; else lo = mid + 1;
   }
-  const uint64_t c = lo;
+  const uint64_t c = lo, ns = cs / ss;
   double r = cb[c];
-  uint64_t outcome = ~0ull, last_pos = c * cs;
-  for (uint64_t j = 0; j < cs; ++j) {
-    const double pj = prob_exact(re, im, c * cs + j);
-    if (pj > 0.0) last_pos = c * cs + j;
-    r = dadd(r, pj);
-    if (r > target) {
-      outcome = c * cs + j;
+  uint64_t kk = ns;
+  for (uint64_t q = 0; q < ns; ++q) {
+    const double rn = dadd(r, subs[c * ns + q]);
+    if (rn > target) {
+      kk = q;
       break;
     }
+    r = rn;
   }
-  out[k] = outcome == ~0ull ? last_pos : outcome;
+  uint64_t outcome = ~0ull;
+  if (kk < ns) {
+    uint64_t last_pos = ~0ull;
+    for (uint64_t j = 0; j < ss; ++j) {
+      const uint64_t i = c * cs + kk * ss + j;
+      const double pj = prob_exact(re, im, i);
+      if (pj > 0.0) last_pos = i;
+      r = dadd(r, pj);
+      if (r > target) {
+        outcome = i;
+        break;
+      }
+    }
+    if (outcome == ~0ull) outcome = last_pos;
+  }
+  if (outcome == ~0ull) {  // the last index of the chunk with p > 0, or its first
+    outcome = c * cs;
+    for (uint64_t j = cs; j-- > 0;)
+      if (prob_exact(re, im, c * cs + j) > 0.0) {
+        outcome = c * cs + j;
+        break;
+      }
+  }
+  out[k] = outcome;
 }
 
 int sample(spz_state_t h, const double* u, size_t nshots, uint64_t* out) {
   if (!u || !out) return fail(SPZ_ERR_NULL, "NULL argument");
   if (nshots == 0) return SPZ_OK;
   const uint64_t cs = std::min<uint64_t>(h->N, kChunk);
+  const uint64_t ss = std::min<uint64_t>(cs, kSub);
   const uint64_t nchunks = h->N / cs;
   const uint64_t nsuper = (nchunks + kSuper - 1) / kSuper;
-  // scratch: ct[nchunks] cb[nchunks] ce[nchunks] st[nsuper] sb[nsuper] total[1] u[nshots] out[nshots]
-  const size_t doubles = 3 * nchunks + 2 * nsuper + 8 + 2 * nshots;
+  // scratch: subs[N/ss] ct[nchunks] cb[nchunks] ce[nchunks] st[nsuper] sb[nsuper] total[1] u[nshots] out[nshots]
+  const size_t doubles = h->N / ss + 3 * nchunks + 2 * nsuper + 8 + 2 * nshots;
   void* scratch;
   int rc = ensure_dev_scratch(h, doubles * sizeof(double), &scratch);
   if (rc) return rc;
-  double* ct = (double*)scratch;
+  double* subs = (double*)scratch;
+  double* ct = subs + h->N / ss;
   double* cb = ct + nchunks;
   double* ce = cb + nchunks;
   double* st = ce + nchunks;
@@ -763,12 +796,12 @@ int sample(spz_state_t h, const double* u, size_t nshots, uint64_t* out) {
   uint64_t* dout = (uint64_t*)(du + nshots);
   SPZ_CUDA(cudaMemcpyAsync(du, u, nshots * sizeof(double), cudaMemcpyDefault, h->stream));
   const int cblocks = (int)std::min<uint64_t>((nchunks + 127) / 128, (uint64_t)kNumSMs * 16);
-  chunk_total_kernel<<<cblocks, 128, 0, h->stream>>>(h->re, h->im, nchunks, cs, ct);
+  chunk_total_kernel<<<cblocks, 128, 0, h->stream>>>(h->re, h->im, nchunks, cs, ss, ct, subs);
   super_total_kernel<<<(unsigned)((nsuper + 127) / 128), 128, 0, h->stream>>>(ct, nchunks, nsuper, st);
   super_base_kernel<<<1, 1, 0, h->stream>>>(st, nsuper, sb, total);
   chunk_base_kernel<<<(unsigned)((nsuper + 127) / 128), 128, 0, h->stream>>>(ct, sb, total, nchunks, nsuper, cb, ce);
-  sample_kernel<<<(unsigned)((nshots + 255) / 256), 256, 0, h->stream>>>(h->re, h->im, nchunks, cs, cb, ce, total,
-                                                                         du, nshots, dout);
+  sample_kernel<<<(unsigned)((nshots + 255) / 256), 256, 0, h->stream>>>(h->re, h->im, nchunks, cs, ss, subs, cb,
+                                                                         ce, total, du, nshots, dout);
   SPZ_CHECK_LAUNCH("sampling kernels");
   double host_total;
   rc = read_back(h, total, &host_total, 1);
