@@ -1,7 +1,7 @@
 #!/usr/bin/env python3
 """Benchmark: 30-qubit FP64 brickwork circuit on one GB300 (+ adjoint gradients).
 
-Workload (BASELINE config 2): 30 qubits FP64 (16 GiB state), from |0...0>,
+Workload (config 2, the brickwork circuit): 30 qubits FP64 (16 GiB state), from |0...0>,
 20 layers of U(theta, phi, lambda) on every qubit (angles uniform in [0, 2 pi)
 from the seeded splitmix64 stream, seed 2), then CX on (0,1),(2,3),...,(28,29)
 and (1,2),...,(27,28): 1180 gates.  One step = reset to |0...0> + execute the

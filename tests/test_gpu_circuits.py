@@ -2,7 +2,7 @@
 
 The planner only reorders gates where the swap is bit-exact, and each gate's
 arithmetic inside a tile is the plain kernel's, so fused results are expected
-to be bit-identical; the asserted bound is the benchmark spec's 1e-12 plus an exact
+to be bit-identical; the asserted bound is the 1e-12 parity bound plus an exact
 check where the circuit allows it."""
 import math
 

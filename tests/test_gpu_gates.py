@@ -2,7 +2,7 @@
 
 The kernels perform the reference's own floating-point operations in the same
 order, so single-gate results must be bit-identical to the oracle's; the
-assertion is exact equality (the benchmark spec's bound of 1e-12 is implied)."""
+assertion is exact equality (the 1e-12 parity bound is implied)."""
 import itertools
 
 import numpy as np
