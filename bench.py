@@ -225,14 +225,20 @@ def adjoint_bench(n: int = 24, layers: int = 8, fd_sample: int = 4) -> dict:
     H = core.ising_hamiltonian(a, b)
     opsv = adjoint.set_params(ops, pidx, theta)
     s = State(n)
-    adjoint.adjoint_gradient(s, opsv, pidx, H)  # warm-up (allocates the work vectors)
-    torch.cuda.synchronize()
-    reps = 2
-    t0 = time.perf_counter()
-    for _ in range(reps):
+    reps = 3
+
+    def timed(fast):
         s.reset_zero()
-        adjoint.adjoint_gradient(s, opsv, pidx, H)
-    t_adj = (time.perf_counter() - t0) / reps
+        adjoint.adjoint_gradient(s, opsv, pidx, H, fast=fast)  # warm-up (allocates the work vectors)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            s.reset_zero()
+            e, g = adjoint.adjoint_gradient(s, opsv, pidx, H, fast=fast)
+        return (time.perf_counter() - t0) / reps, e, g
+
+    t_exact, e_exact, g_exact = timed(False)
+    t_adj, e_fast, g_fast = timed(True)  # the headline: fast mode
     # FD baseline: forward circuits with the plain per-gate kernels + <H>.
     f = State(n)
     qc = QuantumCircuit.from_state(f, fused=False)
@@ -246,7 +252,10 @@ def adjoint_bench(n: int = 24, layers: int = 8, fd_sample: int = 4) -> dict:
         core.pauli_expectation(f, H)
     t_fwd = (time.perf_counter() - t0) / fd_sample
     t_fd = 2 * len(pidx) * t_fwd
-    return {"qubits": n, "params": int(len(pidx)), "adjoint_s": t_adj, "grads_per_s": len(pidx) / t_adj,
+    return {"qubits": n, "params": int(len(pidx)), "mode": "fast", "adjoint_s": t_adj,
+            "grads_per_s": len(pidx) / t_adj, "adjoint_exact_s": t_exact,
+            "max_abs_grad_diff_fast_vs_exact": float(np.max(np.abs(g_fast - g_exact))),
+            "energy_diff_fast_vs_exact": float(abs(e_fast - e_exact)),
             "fd_forward_s": t_fwd, "fd_s_extrapolated": t_fd, "fd_grads_per_s": len(pidx) / t_fd,
             "speedup_vs_fd": t_fd / t_adj, "fd_sample": f"{fd_sample} of {2 * len(pidx)} forward circuits"}
 
@@ -531,7 +540,8 @@ def workload_batch(args) -> None:
     t_build = time.perf_counter() - t0
     tune = (batch.autotune(insts, reps=1) if args.autotune
             else {"tile_qubits": args.batch_tile, "threads": args.batch_threads})
-    b = batch.Batch(insts, tile_qubits=tune["tile_qubits"], threads=tune["threads"], wide_qubits=args.batch_wide)
+    b = batch.Batch(insts, tile_qubits=tune["tile_qubits"], threads=tune["threads"], wide_qubits=args.batch_wide,
+                    fast=args.batch_fast)
     b.run()
     t0 = time.perf_counter()
     for _ in range(args.steps):
@@ -555,7 +565,7 @@ def workload_batch(args) -> None:
           higher_is_better=True,
           config={"workload": f"{len(insts)} HEA instances (RY/RZ layers + CZ ring), qubits U{{10..{args.batch_qmax}}}, depth "
                               f"U{{2..10}}, seeds 8+k", "params": nparams, "launch": tune,
-                  "wide_qubits": args.batch_wide or 18},
+                  "wide_qubits": args.batch_wide or 18, "wide_adjoint": "fast" if args.batch_fast else "exact"},
           seconds_per_batch=t_batch, grads_per_s=nparams / t_batch, loop_seconds_extrapolated=t_loop,
           loop_sample=len(sample), speedup_vs_loop=t_loop / t_batch, max_abs_energy_diff=max_e,
           max_abs_grad_diff=max_g, build_seconds=t_build, info=b.info())
@@ -614,6 +624,7 @@ def main() -> None:
     ap.add_argument("--batch-tile", type=int, default=12, help="batch workload: tile qubits (resident up to this n)")
     ap.add_argument("--batch-threads", type=int, default=512, help="batch workload: threads per block")
     ap.add_argument("--batch-qmax", type=int, default=22, help="batch workload: largest instance (small profiling cases)")
+    ap.add_argument("--batch-fast", action="store_true", help="batch workload: fast adjoint for the wide instances")
     ap.add_argument("--batch-wide", type=int, default=0,
                     help="batch workload: instances of at least this many qubits run across the whole GPU "
                          "(0: the library default, 31: never)")

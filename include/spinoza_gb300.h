@@ -299,12 +299,15 @@ int spz_sample(spz_state_t h, const double* u, size_t nshots, uint64_t* out);
  * are the rotation gates (P, RX, RY, RZ, and their controlled forms) whose
  * index appears in param_index: param_index[j] = k means d/d(ops[k].gate.p[0])
  * goes to grad[j].  On return the handle holds psi(theta), *energy = E, grad[j]
- * = dE/dtheta_j.  Needs two extra state vectors of device memory.
+ * = dE/dtheta_j.  Needs two extra state vectors of device memory.  flags:
+ * SPZ_EXEC_DEFAULT, or SPZ_EXEC_FAST (fast-mode forward, and a backward sweep
+ * with lazily scaled H / RX / RY inverses and RZ inverses as P: about half the
+ * FP64 work, equal to the exact gradients up to rounding).
  * No reference counterpart (new form built on the gate path). */
 int spz_adjoint_gradient(spz_state_t h, const spz_op* ops, size_t nops,
                          const uint32_t* param_index, size_t nparams,
-                         const spz_pauli_term* terms, size_t nterms, double* energy,
-                         double* grad);
+                         const spz_pauli_term* terms, size_t nterms, uint32_t flags,
+                         double* energy, double* grad);
 
 /* ---------------------------------------------------------------- batching */
 /* Many independent parameterised circuits of uneven qubit counts, each with its
@@ -331,7 +334,8 @@ typedef struct spz_batch_config {
   int32_t wide_qubits;    /* instances of at least this many qubits run one at a time
                              across the whole GPU (fused passes + fused adjoint sweep)
                              instead of one per CTA; 0 = 18, > 30 = never            */
-  int32_t reserved;
+  int32_t flags;          /* SPZ_EXEC_FAST: the wide instances use the fast adjoint
+                             (equal to the exact one up to rounding)                 */
 } spz_batch_config;
 
 typedef struct spz_batch_stats {

@@ -84,7 +84,7 @@ class spz_batch_instance(ctypes.Structure):
 
 
 class spz_batch_config(ctypes.Structure):
-    _fields_ = [("tile_qubits", c_int32), ("threads", c_int32), ("wide_qubits", c_int32), ("reserved", c_int32)]
+    _fields_ = [("tile_qubits", c_int32), ("threads", c_int32), ("wide_qubits", c_int32), ("flags", c_int32)]
 
 
 class spz_batch_stats(ctypes.Structure):
@@ -146,7 +146,7 @@ SIGNATURES = [
     ("spz_norm_sqr", c_int, [c_void_p, POINTER(c_double)]),
     ("spz_sample", c_int, [c_void_p, c_void_p, c_size_t, c_void_p]),
     ("spz_adjoint_gradient", c_int, [c_void_p, c_void_p, c_size_t, c_void_p, c_size_t, c_void_p, c_size_t,
-                                     POINTER(c_double), c_void_p]),
+                                     c_uint32, POINTER(c_double), c_void_p]),
     ("spz_batch_create", c_int, [c_void_p, c_size_t, c_void_p, c_void_p, c_void_p, POINTER(spz_batch_config),
                                  POINTER(c_void_p)]),
     ("spz_batch_run", c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),

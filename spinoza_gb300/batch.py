@@ -68,12 +68,15 @@ def pack(instances: Sequence[Instance]):
 class Batch:
     """A planned, device-resident batch; run(theta) -> (energies, grads)."""
 
-    def __init__(self, instances: Sequence[Instance], tile_qubits: int = 0, threads: int = 0, wide_qubits: int = 0):
+    def __init__(self, instances: Sequence[Instance], tile_qubits: int = 0, threads: int = 0, wide_qubits: int = 0,
+                 fast: bool = False):
         """tile_qubits / threads: launch shape of the persistent kernel;
         wide_qubits: instances of at least this many qubits run one at a time
-        across the whole GPU (0: the library's default, 31: never)."""
+        across the whole GPU (0: the library's default, 31: never); fast: those
+        use the fast adjoint (equal to the exact one up to rounding)."""
         self.inst, self.ops, self.pidx, self.theta, self.terms = pack(instances)
-        cfg = nat.spz_batch_config(int(tile_qubits), int(threads), int(wide_qubits), 0)
+        cfg = nat.spz_batch_config(int(tile_qubits), int(threads), int(wide_qubits),
+                                   nat.EXEC_FAST if fast else nat.EXEC_DEFAULT)
         h = c_void_p()
         nat.check(nat.lib().spz_batch_create(nat.ptr(self.inst), len(self.inst), nat.ptr(self.ops),
                                              nat.ptr(self.pidx), nat.ptr(self.terms), byref(cfg), byref(h)))

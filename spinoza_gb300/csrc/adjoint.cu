@@ -24,6 +24,8 @@
 // diagonal / non-diagonal roles), so each gradient still sees the states it
 // would see in program order.
 #include <algorithm>
+#include <cmath>
+#include <complex>
 #include <cstring>
 #include <vector>
 
@@ -179,8 +181,13 @@ __device__ __forceinline__ double adj_pair(const TileGate& g, int mode, double* 
     double a = pr[s0], b = pi[s0], c = pr[s1], d = pi[s1];
     double p = lr[s0], q = li[s0], r = lr[s1], s = li[s1];
     if (mode >= 0) acc = dadd(acc, adj_pair_term(mode, a, b, c, d, p, q, r, s));
-    gate_pair<KIND>(cf, a, b, c, d);
-    gate_pair<KIND>(cf, p, q, r, s);
+    if constexpr (KIND >= FK_LAZY_H) {
+      fast_pair<KIND>(cf, a, b, c, d);
+      fast_pair<KIND>(cf, p, q, r, s);
+    } else {
+      gate_pair<KIND>(cf, a, b, c, d);
+      gate_pair<KIND>(cf, p, q, r, s);
+    }
     pr[s0] = a; pi[s0] = b; pr[s1] = c; pi[s1] = d;
     lr[s0] = p; li[s0] = q; lr[s1] = r; li[s1] = s;
   }
@@ -278,6 +285,11 @@ __global__ void __launch_bounds__(kAdjTileThreads) adj_tile_kernel(AdjPassArgs A
             case SPZ_GATE_Y: v = adj_pair_any<SPZ_GATE_Y>(g, mode, pr, pi, lr, li, nw); break;
             case SPZ_GATE_RX: v = adj_pair_any<SPZ_GATE_RX>(g, mode, pr, pi, lr, li, nw); break;
             case SPZ_GATE_RY: v = adj_pair_any<SPZ_GATE_RY>(g, mode, pr, pi, lr, li, nw); break;
+            case FK_LAZY_H: v = adj_pair_any<FK_LAZY_H>(g, mode, pr, pi, lr, li, nw); break;
+            case FK_LAZY_RX_A: v = adj_pair_any<FK_LAZY_RX_A>(g, mode, pr, pi, lr, li, nw); break;
+            case FK_LAZY_RX_B: v = adj_pair_any<FK_LAZY_RX_B>(g, mode, pr, pi, lr, li, nw); break;
+            case FK_LAZY_RY_A: v = adj_pair_any<FK_LAZY_RY_A>(g, mode, pr, pi, lr, li, nw); break;
+            case FK_LAZY_RY_B: v = adj_pair_any<FK_LAZY_RY_B>(g, mode, pr, pi, lr, li, nw); break;
             default: v = adj_pair_any<SPZ_GATE_U>(g, mode, pr, pi, lr, li, nw); break;
           }
           break;
@@ -383,9 +395,10 @@ spz_gate inverse_gate(const spz_gate& g) {
 // With d_energy / d_grad (device pointers) the results are written there and
 // nothing waits for the device; otherwise they come back to energy / grad.
 int adjoint_gradient(spz_state_t h, const spz_op* ops, size_t nops, const uint32_t* param_index, size_t nparams,
-                     const spz_pauli_term* terms, size_t nterms, double* energy, double* grad, double* d_energy,
-                     double* d_grad) {
+                     const spz_pauli_term* terms, size_t nterms, uint32_t flags, double* energy, double* grad,
+                     double* d_energy, double* d_grad) {
   const bool on_device = d_energy != nullptr;
+  const bool fast = (flags & SPZ_EXEC_FAST) != 0;
   if (nops && !ops) return fail(SPZ_ERR_NULL, "ops is NULL");
   if (nparams && (!param_index || (on_device ? !d_grad : !grad))) return fail(SPZ_ERR_NULL, "param_index/grad is NULL");
   if (nterms && !terms) return fail(SPZ_ERR_NULL, "terms is NULL");
@@ -435,7 +448,7 @@ int adjoint_gradient(spz_state_t h, const spz_op* ops, size_t nops, const uint32
   std::vector<GateApp> applied;
   for (size_t i = 0; i < nops; ++i)
     if (!skip[i]) applied.push_back(fwd[i]);
-  int rc = run_gates(h, applied, SPZ_EXEC_DEFAULT, nullptr);
+  int rc = run_gates(h, applied, fast ? SPZ_EXEC_FAST : SPZ_EXEC_DEFAULT, nullptr);
   if (rc) return rc;
   rc = ensure_aux(h, 0);
   if (rc) return rc;
@@ -482,6 +495,59 @@ int adjoint_gradient(spz_state_t h, const spz_op* ops, size_t nops, const uint32
     g.src = (int64_t)ii;
     bwd.push_back(g);
   }
+  // Fast mode: uncontrolled H / RX / RY inverses become lazy ops (the gate
+  // divided by a real scalar: 4 FMAs per pair) and uncontrolled RZ inverses
+  // become P (the 1 half only) times a unit phase.  psi and lam pass through
+  // the same ops, so the phases cancel in <lam|K|psi> and the real scalars S
+  // (product so far) enter as S^2 on each gradient.  Above 800 lazy ops S could
+  // leave the exponent range; the sweep then stays exact.
+  std::vector<double> lazy_scale(nops, 1.0);
+  if (fast) {
+    size_t lazy = 0;
+    for (const GateApp& g : bwd)
+      lazy += (g.ones | g.zeros) == 0 &&
+              (g.kind == SPZ_GATE_H || g.kind == SPZ_GATE_RX || g.kind == SPZ_GATE_RY);
+    if (lazy <= 800)
+      for (GateApp& g : bwd) {
+        if ((g.ones | g.zeros) != 0) continue;
+        const int64_t src = g.src;
+        if (g.kind == SPZ_GATE_H) {
+          GateApp l = g;
+          l.kind = FK_LAZY_H;
+          lazy_scale[src] = std::sqrt(0.5);
+          g = l;
+        } else if (g.kind == SPZ_GATE_RX || g.kind == SPZ_GATE_RY) {
+          const bool is_x = g.kind == SPZ_GATE_RX;
+          const double cs = g.c.cs, sn = g.c.sn;  // cos, sin of theta/2
+          GateApp l = g;
+          if (std::fabs(cs) >= std::fabs(sn)) {
+            l.kind = is_x ? FK_LAZY_RX_A : FK_LAZY_RY_A;
+            l.c.cs = sn / cs;
+            lazy_scale[src] = cs;
+          } else {
+            l.kind = is_x ? FK_LAZY_RX_B : FK_LAZY_RY_B;
+            l.c.cs = cs / sn;
+            lazy_scale[src] = sn;
+          }
+          g = l;
+        } else if (g.kind == SPZ_GATE_RZ) {  // RZ = e^{-i theta/2} P(theta): d1 / d0 = e^{i theta}
+          const std::complex<double> d0(g.c.d0re, g.c.d0im), d1(g.c.d1re, g.c.d1im);
+          spz_gate pg{};
+          pg.kind = SPZ_GATE_P;
+          pg.p[0] = std::arg(d1 / d0);
+          GateApp l;
+          rc = make_gate_app(n, pg, g.target, 0, 0, &l);
+          if (rc) return rc;
+          l.src = src;
+          g = l;
+          // P visits only the target's 1 half, so RZ's gradient is taken in
+          // P's form: Im<lam|psi> is 0 (H is Hermitian, and psi, lam pass
+          // through the same unitaries), so sum over the 0 half minus sum over
+          // the 1 half of Im(conj(lam) psi) equals -2 x the 1-half sum.
+          if (mode_of[src] == GM_Z) mode_of[src] = GM_P1;
+        }
+      }
+  }
   const int k = std::min<int>((int)n, kAdjTileK);
   const int c = std::min<int>(kTileLowBits, k);
   std::vector<PlannedPass> passes;
@@ -500,6 +566,17 @@ int adjoint_gradient(spz_state_t h, const spz_op* ops, size_t nops, const uint32
       slots += grad;
     }
     if (!cur.gates.empty()) passes.push_back(std::move(cur));
+  }
+  // S^2 for each differentiated op: S = product of the lazy scalars applied
+  // before its gradient, in the order the passes run.
+  std::vector<double> grad_scale(nops, 1.0);
+  {
+    double S = 1.0;
+    for (const PlannedPass& P : passes)
+      for (const GateApp& g : P.gates) {
+        if (mode_of[g.src] >= 0) grad_scale[g.src] = S * S;
+        S *= lazy_scale[g.src];
+      }
   }
   std::vector<TileGate> tg;
   std::vector<AdjOp> ao;
@@ -550,7 +627,7 @@ int adjoint_gradient(spz_state_t h, const spz_op* ops, size_t nops, const uint32
   std::vector<double> gmul(nparams);
   for (size_t j = 0; j < nparams; ++j) {
     gsel[j] = (int32_t)(1 + param_index[j]);
-    gmul[j] = mode_of[param_index[j]] == GM_P1 ? -2.0 : 1.0;
+    gmul[j] = (mode_of[param_index[j]] == GM_P1 ? -2.0 : 1.0) * grad_scale[param_index[j]];
   }
   const size_t gs_bytes = (nparams * sizeof(int32_t) + 255) / 256 * 256;
   const size_t gm_bytes = nparams * sizeof(double);
@@ -622,7 +699,7 @@ int adjoint_gradient(spz_state_t h, const spz_op* ops, size_t nops, const uint32
   for (size_t j = 0; j < nparams; ++j) {
     const uint32_t k = param_index[j];
     const double im = host[1 + k];
-    grad[j] = mode_of[k] == GM_P1 ? -2.0 * im : im;
+    grad[j] = (mode_of[k] == GM_P1 ? -2.0 * im : im) * grad_scale[k];
   }
   return SPZ_OK;
 }
@@ -632,8 +709,8 @@ int adjoint_gradient(spz_state_t h, const spz_op* ops, size_t nops, const uint32
 using namespace spz;
 
 extern "C" int spz_adjoint_gradient(spz_state_t h, const spz_op* ops, size_t nops, const uint32_t* param_index,
-                                    size_t nparams, const spz_pauli_term* terms, size_t nterms, double* energy,
-                                    double* grad) {
+                                    size_t nparams, const spz_pauli_term* terms, size_t nterms, uint32_t flags,
+                                    double* energy, double* grad) {
   if (!h) return fail(SPZ_ERR_NULL, "handle is NULL");
-  return adjoint_gradient(h, ops, nops, param_index, nparams, terms, nterms, energy, grad, nullptr, nullptr);
+  return adjoint_gradient(h, ops, nops, param_index, nparams, terms, nterms, flags, energy, grad, nullptr, nullptr);
 }

@@ -474,6 +474,7 @@ struct BatchImpl {
   int device = 0;
   int kmax = kBatchMaxK, threads = 512;
   int wide_qubits = kDefaultWideQubits;
+  uint32_t wide_flags = 0;            // SPZ_EXEC_FAST: wide instances use the fast adjoint
   uint32_t nnarrow = 0;               // instances in the persistent kernel
   std::vector<WideInst> wide;         // the others, largest first
   // Wide instances run on kWideStreams streams at once (a pass of one 20-22
@@ -872,6 +873,7 @@ int spz_batch_create(const spz_batch_instance* instances, size_t ninstances, con
     if (config->tile_qubits) b->kmax = config->tile_qubits;
     if (config->threads) b->threads = config->threads;
     if (config->wide_qubits) b->wide_qubits = config->wide_qubits;
+    b->wide_flags = (uint32_t)config->flags & SPZ_EXEC_FAST;
   }
   if (b->kmax < 4 || b->kmax > kBatchMaxK || b->threads < 64 || b->threads > 1024 || (b->threads & 31)) {
     delete b;
@@ -928,7 +930,8 @@ int spz_batch_run(spz_batch_t b, const double* theta, double* energies, double* 
     int rc = spz_state_reset_zero(h);
     if (!rc)
       rc = adjoint_gradient(h, w.ops.data(), w.ops.size(), w.pidx.data(), w.pidx.size(), w.terms.data(),
-                            w.terms.size(), nullptr, nullptr, b->d_energy + w.idx, b->d_grad + w.param_offset);
+                            w.terms.size(), b->wide_flags, nullptr, nullptr, b->d_energy + w.idx,
+                            b->d_grad + w.param_offset);
     if (rc) {
       wait_all();
       return rc;

@@ -186,8 +186,8 @@ std::vector<PlannedPass> plan_passes(const std::vector<GateApp>& gates, uint32_t
 // Adjoint gradient of <psi|H|psi> on h (adjoint.cu); with d_energy / d_grad
 // (device) the results stay on the device and nothing waits for it.
 int adjoint_gradient(spz_state_t h, const spz_op* ops, size_t nops, const uint32_t* param_index, size_t nparams,
-                     const spz_pauli_term* terms, size_t nterms, double* energy, double* grad, double* d_energy,
-                     double* d_grad);
+                     const spz_pauli_term* terms, size_t nterms, uint32_t flags, double* energy, double* grad,
+                     double* d_energy, double* d_grad);
 
 // Reductions used by measurement and the executor.
 int prob0_device(spz_state_t h, uint32_t target, double* out);

@@ -1,8 +1,7 @@
 """Adjoint gradients vs the oracle's parameter shift and vs central differences.
 
 Parameter shift is exact for RY/RZ (dE/dtheta = [E(theta + pi/2) - E(theta - pi/2)] / 2),
-so it pins the gradient to rounding level; the tolerance written here is the
-north-star's 1e-9."""
+so it pins the gradient to rounding level; the tolerance written here is 1e-9."""
 import math
 
 import numpy as np
@@ -43,6 +42,67 @@ def test_adjoint_matches_oracle_parameter_shift(gpu, n, layers):
         ps = 0.5 * (_oracle_energy(n, adjoint.set_params(ops, pidx, tp), H)
                     - _oracle_energy(n, adjoint.set_params(ops, pidx, tm), H))
         assert abs(g[j] - ps) < 1e-9, (j, g[j], ps)
+
+
+def _mixed_circuit(n, seed):
+    """H, RX, RY, RZ, P, controlled rotations and CZ, with parameters on every
+    rotation (the fast sweep turns the uncontrolled ones into lazy ops / P)."""
+    from spinoza_gb300 import _native as nat
+
+    r = np.random.default_rng(seed)
+    rows, pidx = [], []
+    for layer in range(3):
+        for q in range(n):
+            k = [nat.H, nat.RX, nat.RY, nat.RZ, nat.P][(q + layer) % 5]
+            if k != nat.H:
+                pidx.append(len(rows))
+            rows.append(((k, 0, 0, 0, (r.uniform(-3, 3), 0, 0)), q, nat.CONTROLS_NONE, 0, 0))
+        for q in range(n - 1):
+            k = [nat.RY, nat.RZ, nat.Z][(q + layer) % 3]
+            if k != nat.Z:
+                pidx.append(len(rows))
+            rows.append(((k, 0, 0, 0, (r.uniform(-3, 3), 0, 0)), q + 1, nat.CONTROLS_SINGLE, 1 << q, 0))
+    ops = np.zeros(len(rows), dtype=nat.OP_DTYPE)
+    for i, row in enumerate(rows):
+        ops[i] = row
+    return ops, np.array(pidx, dtype=np.uint32)
+
+
+@pytest.mark.parametrize("n", [3, 7, 12])
+def test_fast_adjoint_equals_exact_and_parameter_shift(gpu, n):
+    """Fast mode (lazy inverses, RZ as P, scale folded into the gradients)
+    gives the exact adjoint's numbers up to rounding, and the oracle's
+    parameter-shift gradients within 1e-9."""
+    ops, pidx = _mixed_circuit(n, 40 + n)
+    _, _, _, H = _problem(n, 1, 9)
+    e0, g0 = adjoint.adjoint_gradient(State(n), ops, pidx, H)
+    e1, g1 = adjoint.adjoint_gradient(State(n), ops, pidx, H, fast=True)
+    assert abs(e1 - e0) < 1e-12
+    np.testing.assert_allclose(g1, g0, atol=1e-12, rtol=0)
+    theta = ops["gate"]["p"][pidx.astype(np.int64), 0].copy()
+    for j in range(0, len(pidx), max(1, len(pidx) // 6)):
+        if ops["gate"]["kind"][pidx[j]] == 5 or ops["controls_kind"][pidx[j]] != 0:
+            continue  # parameter shift with +-pi/2 is exact for uncontrolled RX/RY/RZ only
+        tp, tm = theta.copy(), theta.copy()
+        tp[j] += math.pi / 2
+        tm[j] -= math.pi / 2
+        ps = 0.5 * (_oracle_energy(n, adjoint.set_params(ops, pidx, tp), H) -
+                    _oracle_energy(n, adjoint.set_params(ops, pidx, tm), H))
+        assert abs(g1[j] - ps) < 1e-9, (j, g1[j], ps)
+
+
+def test_fast_adjoint_falls_back_to_exact_for_very_deep_circuits(gpu):
+    """More than 800 lazy inverses: the sweep stays exact (the scale would
+    leave the exponent range); results still match the exact adjoint."""
+    n, layers = 3, 300
+    ops, pidx = adjoint.hardware_efficient_ansatz(n, layers)
+    theta = (rng.uniforms(3, len(pidx)) * 2 - 1) * math.pi
+    _, _, _, H = _problem(n, 1, 9)
+    opsv = adjoint.set_params(ops, pidx, theta)
+    e0, g0 = adjoint.adjoint_gradient(State(n), opsv, pidx, H)
+    e1, g1 = adjoint.adjoint_gradient(State(n), opsv, pidx, H, fast=True)
+    assert abs(e1 - e0) < 1e-12
+    np.testing.assert_allclose(g1, g0, atol=1e-11, rtol=0)
 
 
 def test_adjoint_matches_central_differences_on_gpu(gpu):
