@@ -81,17 +81,18 @@ def _torch_function():
         """E(theta) = <0|U(theta)^dagger H U(theta)|0>; backward by adjoint differentiation."""
 
         @staticmethod
-        def forward(ctx, theta, n: int, ops: np.ndarray, param_index: np.ndarray, terms: np.ndarray):
+        def forward(ctx, theta, n: int, ops: np.ndarray, param_index: np.ndarray, terms: np.ndarray,
+                    fast: bool = False):
             th = theta.detach().to("cpu", torch.float64).numpy()
             s = State(n)
-            e, g = adjoint_gradient(s, set_params(ops, param_index, th), param_index, terms)
+            e, g = adjoint_gradient(s, set_params(ops, param_index, th), param_index, terms, fast=fast)
             ctx.save_for_backward(torch.from_numpy(g).to(theta.device))
             return torch.tensor(e, dtype=torch.float64, device=theta.device)
 
         @staticmethod
         def backward(ctx, grad_out):
             (g,) = ctx.saved_tensors
-            return grad_out * g, None, None, None, None
+            return grad_out * g, None, None, None, None, None
 
     return AdjointExpectation
 
@@ -99,13 +100,15 @@ def _torch_function():
 _fn = None
 
 
-def energy(theta, n: int, ops: np.ndarray, param_index: np.ndarray, terms) -> "torch.Tensor":  # noqa: F821
-    """Differentiable E(theta) as a torch scalar (float64)."""
+def energy(theta, n: int, ops: np.ndarray, param_index: np.ndarray, terms,
+           fast: bool = False) -> "torch.Tensor":  # noqa: F821
+    """Differentiable E(theta) as a torch scalar (float64); fast=True uses the
+    fast adjoint (equal to the exact gradients up to rounding)."""
     global _fn
     if _fn is None:
         _fn = _torch_function()
     arr = terms if isinstance(terms, np.ndarray) else pauli_terms(terms)
-    return _fn.apply(theta, n, ops, param_index, arr)
+    return _fn.apply(theta, n, ops, param_index, arr, fast)
 
 
 _ = (math, Optional, Sequence)

@@ -158,3 +158,16 @@ def test_torch_autograd_function(gpu):
     _, g = adjoint.adjoint_gradient(State(n), adjoint.set_params(ops, pidx, theta), pidx, H)
     assert abs(e.item() - _oracle_energy(n, adjoint.set_params(ops, pidx, theta), H)) < 1e-12
     np.testing.assert_array_equal(t.grad.numpy(), g)
+
+
+def test_torch_autograd_function_fast(gpu):
+    import torch
+
+    n, layers = 6, 2
+    ops, pidx, theta, H = _problem(n, layers, 10)
+    t = torch.tensor(theta, dtype=torch.float64, requires_grad=True)
+    e = adjoint.energy(t, n, ops, pidx, H, fast=True)
+    e.backward()
+    _, g = adjoint.adjoint_gradient(State(n), adjoint.set_params(ops, pidx, theta), pidx, H)
+    assert abs(e.item() - _oracle_energy(n, adjoint.set_params(ops, pidx, theta), H)) < 1e-12
+    np.testing.assert_allclose(t.grad.numpy(), g, atol=1e-12, rtol=0)
