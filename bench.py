@@ -555,7 +555,8 @@ def workload_batch(args) -> None:
     for i in sample:
         n, ops, pidx, theta, terms = insts[i]
         t1 = time.perf_counter()
-        e1, g1 = adjoint.adjoint_gradient(State(n), adjoint.set_params(ops, pidx, theta), pidx, terms)
+        e1, g1 = adjoint.adjoint_gradient(State(n), adjoint.set_params(ops, pidx, theta), pidx, terms,
+                                          fast=args.batch_fast)
         t_loop_sample += time.perf_counter() - t1
         max_e = max(max_e, abs(e1 - e[i]))
         max_g = max(max_g, float(np.max(np.abs(g1 - b.split(g)[i]))))
