@@ -221,6 +221,21 @@ int spz_circuit_execute_host(spz_state_t h, const double* in_reals, const double
                              double* out_imags, const spz_op* ops, size_t nops, spz_tracker* tracker,
                              uint32_t flags, spz_exec_stats* stats);
 
+/* Compiled circuits: plan `ops` once for n qubits (fused passes; fast-mode
+ * lowering with SPZ_EXEC_FAST; descriptors uploaded to device memory the
+ * program owns) and run it on any n-qubit state as a replayed CUDA graph: a
+ * run costs no planning and no host work beyond one graph launch on the
+ * state's stream (asynchronous; spz_state_synchronize waits).  The graph is
+ * captured on the first run for a given state and again when the state
+ * changes.  Programs hold no measurements (SPZ_ERR_UNSUPPORTED); a Single
+ * control is always a quantum control.  Extension: the reference plans nothing
+ * ahead (QuantumCircuit::execute, circuit.rs:552-600, walks the list each time). */
+typedef struct spz_program_s* spz_program_t;
+int spz_program_create(uint32_t n, const spz_op* ops, size_t nops, uint32_t flags, spz_program_t* out);
+int spz_program_run(spz_program_t p, spz_state_t h);
+int spz_program_stats(spz_program_t p, spz_exec_stats* stats);
+int spz_program_destroy(spz_program_t p);
+
 /* Plan `ops` for an n-qubit state without running anything (host only; no
  * device is needed): fills the counters spz_circuit_execute would, taking every
  * measurement outcome as 0.  For inspecting how a circuit is fused. */

@@ -132,6 +132,10 @@ SIGNATURES = [
                                     POINTER(spz_exec_stats)]),
     ("spz_circuit_execute_host", c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_size_t,
                                          POINTER(spz_tracker), c_uint32, POINTER(spz_exec_stats)]),
+    ("spz_program_create", c_int, [c_uint32, c_void_p, c_size_t, c_uint32, POINTER(c_void_p)]),
+    ("spz_program_run", c_int, [c_void_p, c_void_p]),
+    ("spz_program_stats", c_int, [c_void_p, POINTER(spz_exec_stats)]),
+    ("spz_program_destroy", c_int, [c_void_p]),
     ("spz_plan_stats", c_int, [c_uint32, c_void_p, c_size_t, c_uint32, POINTER(spz_exec_stats)]),
     ("spz_plan_schedule", c_int, [c_uint32, c_void_p, c_size_t, c_uint32, c_void_p, c_void_p, c_size_t,
                                   POINTER(c_size_t)]),

@@ -345,6 +345,39 @@ def execute_host(ops: np.ndarray, reals: np.ndarray, imags: np.ndarray, out: Opt
     return st
 
 
+class Program:
+    """A circuit planned once and replayed as a CUDA graph (spz_program_*):
+    ``Program(n, ops).run(state)`` applies `ops` to an n-qubit state with no
+    planning or uploads per run.  No measurements; fused / fast as in
+    QuantumCircuit.  Runs are asynchronous on the state's stream."""
+
+    def __init__(self, n: int, ops: np.ndarray, fused: bool = True, fast: bool = False):
+        self.n = int(n)
+        ops = np.ascontiguousarray(ops, dtype=nat.OP_DTYPE)
+        h = nat.c_void_p()
+        nat.check(nat.lib().spz_program_create(self.n, nat.ptr(ops), len(ops), _flags(fused, fast), byref(h)))
+        self._h = h
+
+    def run(self, state: State) -> None:
+        nat.check(nat.lib().spz_program_run(self._h, state.handle))
+
+    def stats(self) -> dict:
+        st = nat.spz_exec_stats()
+        nat.check(nat.lib().spz_program_stats(self._h, byref(st)))
+        return {f: getattr(st, f) for f, _ in nat.spz_exec_stats._fields_}
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            nat.lib().spz_program_destroy(self._h)
+            self._h = nat.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def _flags(fused: bool, fast: bool) -> int:
     if fast:
         return nat.EXEC_FAST

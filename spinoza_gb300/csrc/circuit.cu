@@ -511,6 +511,32 @@ uint64_t op_fp64_ops(uint32_t n, const GateApp& g, const std::vector<PhaseTable>
   return gate_fp64_ops(n, g);
 }
 
+// Resident blocks per SM for a tile pass of `threads` x `smem` and the SM
+// count; the grid of a tile pass is one wave of them (each block loops over
+// tiles), so no block waits for a second wave.  Cached per tile size.
+int tile_launch_shape(int device, int threads, size_t smem, int* resident_out, int* sms_out) {
+  static int sms = 0;
+  static int resident[kTileMaxK + 2] = {};  // by log2 of the tile
+  if (!sms) {
+    SPZ_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+    const int max_smem = (2 << kTileMaxK) * 8 + (1 << (kTileMaxK - kTileLowBits)) * 8;
+    SPZ_CUDA(cudaFuncSetAttribute(tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+    SPZ_CUDA(cudaFuncSetAttribute(tile_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                  cudaSharedmemCarveoutMaxShared));
+  }
+  int lg = 0;  // the largest lg with 2 x 8 B x 2^lg <= smem (the tile's re and im)
+  while (lg <= kTileMaxK && (16ull << (lg + 1)) <= smem) ++lg;
+  int& r = resident[lg];
+  if (!r) {
+    int per_sm = 0;
+    SPZ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tile_kernel, threads, smem));
+    r = std::max(1, per_sm);
+  }
+  *resident_out = r;
+  *sms_out = sms;
+  return SPZ_OK;
+}
+
 // Host arrays that one run of gates uploads from before it and downloads to
 // after it, with the copies overlapping the first and last tile pass where the
 // pass can be cut into kIoChunks slabs: slab j holds the amplitudes whose
@@ -689,19 +715,7 @@ int run_gates_io(spz_state_t h, const std::vector<GateApp>& gates_in, uint32_t f
     dgates = (TileGate*)dscr;
     dtables = (const double2*)((char*)dscr + gbytes);
   }
-  // Resident blocks per SM for the full-size tile; the grid is one wave of them
-  // (each block loops over tiles), so no block waits for a second wave.
-  static int resident = 0, sms = kNumSMs;
-  if (!resident) {
-    SPZ_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device));
-    const int max_smem = (2 << kTileMaxK) * 8 + (1 << (kTileMaxK - kTileLowBits)) * 8;
-    SPZ_CUDA(cudaFuncSetAttribute(tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
-    SPZ_CUDA(cudaFuncSetAttribute(tile_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                  cudaSharedmemCarveoutMaxShared));
-    int per_sm = 0;
-    SPZ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tile_kernel, kTileThreads, max_smem));
-    resident = std::max(1, per_sm);
-  }
+
   auto pass_slab_q = [&](const PlannedPass& P) -> int {
     if (!io || n < 3 || !tiled(P) || (n - P.local.size()) < 3) return -1;
     uint64_t local_mask = 0;
@@ -746,6 +760,11 @@ int run_gates_io(spz_state_t h, const std::vector<GateApp>& gates_in, uint32_t f
     const uint32_t T = 1u << A.k;
     const size_t smem = 2 * T * sizeof(double) + (size_t)(1u << A.nhigh) * sizeof(uint64_t);
     const int threads = (int)std::min<uint32_t>(kTileThreads, std::max<uint32_t>(32, T / 2));
+    int resident = 0, sms = 0;
+    {
+      int rc2 = tile_launch_shape(h->device, threads, smem, &resident, &sms);
+      if (rc2) return rc2;
+    }
     // With host copies to overlap, the first / last pass runs slab by slab
     // (the first pass only in the geometry its uploads were queued in).
     const int sq = pass_slab_q(P);
@@ -1032,6 +1051,193 @@ int plan_stats(uint32_t n, const spz_op* ops, size_t nops, uint32_t flags, spz_e
   return SPZ_OK;
 }
 
+// ------------------------------------------------------------ programs
+// A circuit planned once: lowered (fast mode), fused into passes, its tile
+// descriptors and phase tables uploaded to device memory it owns.  A run
+// replays the launches as a CUDA graph captured per target state (the graph
+// holds the state's device pointers), so a repeated run costs no planning,
+// no uploads and one graph launch.
+struct ProgramPass {
+  bool tiled = false;
+  GateApp plain{};     // !tiled: the one exact gate, through the plain kernel
+  PassArgs args{};     // tiled: everything but the state pointers
+  int threads = 0;
+  size_t smem = 0;
+  uint64_t blocks = 0;
+};
+
+}  // namespace spz
+
+struct spz_program_s {
+  uint32_t n = 0;
+  int device = 0;
+  std::vector<spz::ProgramPass> passes;
+  void* dbuf = nullptr;            // tile descriptors + phase tables
+  cudaStream_t capture = nullptr;  // private stream the graph is captured on
+  cudaGraphExec_t exec = nullptr;  // the captured launches ...
+  double* exec_re = nullptr;       // ... for this state
+  double* exec_im = nullptr;
+  spz_exec_stats stats{};
+};
+
+namespace spz {
+namespace {
+
+void free_program(spz_program_t p) {
+  if (!p) return;
+  if (p->exec) cudaGraphExecDestroy(p->exec);
+  if (p->capture) cudaStreamDestroy(p->capture);
+  if (p->dbuf) cudaFree(p->dbuf);
+  delete p;
+}
+
+int build_program(spz_program_t p, const spz_op* ops, size_t nops, uint32_t flags) {
+  const uint32_t n = p->n;
+  spz_state_s fake;  // op validation needs only n
+  fake.n = n;
+  fake.N = 1ull << n;
+  spz_tracker tr{};
+  std::vector<GateApp> gates_in;
+  for (size_t i = 0; i < nops; ++i) {
+    const spz_op& op = ops[i];
+    if (op.gate.kind == SPZ_GATE_M) return fail(SPZ_ERR_UNSUPPORTED, "a program cannot hold measurements");
+    bool skip;
+    GateApp a;
+    int rc = op_to_app(&fake, op, tr, 0, &skip, &a);
+    if (rc) return rc;
+    if (skip) continue;
+    a.src = (int64_t)i;
+    gates_in.push_back(a);
+    p->stats.gates++;
+    p->stats.algorithmic_bytes += gate_algorithmic_bytes(n, a);
+  }
+  const bool fast = (flags & SPZ_EXEC_FAST) != 0;
+  std::vector<GateApp> lowered;
+  std::vector<PhaseTable> tables;
+  if (fast) lower_fast(gates_in, n, &lowered, &tables);
+  const std::vector<GateApp>& gates = fast ? lowered : gates_in;
+  for (const GateApp& g : gates) p->stats.fp64_ops += op_fp64_ops(n, g, tables);
+  if ((flags & SPZ_EXEC_UNFUSED) && !fast) {
+    for (const GateApp& g : gates) {
+      ProgramPass pp;
+      pp.plain = g;
+      p->passes.push_back(pp);
+      p->stats.passes++;
+      p->stats.bytes_moved += gate_algorithmic_bytes(n, g);
+    }
+    return SPZ_OK;
+  }
+  const int k = std::min<int>((int)n, kTileMaxK);
+  const int c = std::min<int>(kTileLowBits, k);
+  std::vector<PlannedPass> planned = plan(gates, n, k, c, !fast);
+  std::vector<uint32_t> table_offsets;
+  std::vector<double> flat;
+  for (const PhaseTable& t : tables) {
+    table_offsets.push_back((uint32_t)(flat.size() / 2));
+    for (size_t i = 0; i < t.re.size(); ++i) {
+      flat.push_back(t.re[i]);
+      flat.push_back(t.im[i]);
+    }
+  }
+  std::vector<TileGate> all;
+  std::vector<size_t> offs;
+  for (const PlannedPass& P : planned) {
+    offs.push_back(all.size());
+    const bool tiled = P.gates.size() > 1 || P.gates[0].kind >= FK_LAZY_H || P.gates[0].cond >= 0;
+    if (tiled)
+      for (const GateApp& g : P.gates) all.push_back(tile_gate(g, P.local, &tables, &table_offsets));
+  }
+  const size_t gbytes = (all.size() * sizeof(TileGate) + 255) / 256 * 256;
+  const size_t tbytes = flat.size() * sizeof(double);
+  if (gbytes + tbytes) {
+    SPZ_CUDA(cudaMalloc(&p->dbuf, gbytes + tbytes));
+    if (!all.empty())
+      SPZ_CUDA(cudaMemcpy(p->dbuf, all.data(), all.size() * sizeof(TileGate), cudaMemcpyHostToDevice));
+    if (tbytes) SPZ_CUDA(cudaMemcpy((char*)p->dbuf + gbytes, flat.data(), tbytes, cudaMemcpyHostToDevice));
+  }
+
+  for (size_t q = 0; q < planned.size(); ++q) {
+    const PlannedPass& P = planned[q];
+    ProgramPass pp;
+    pp.tiled = P.gates.size() > 1 || P.gates[0].kind >= FK_LAZY_H || P.gates[0].cond >= 0;
+    p->stats.passes++;
+    if (!pp.tiled) {
+      pp.plain = P.gates[0];
+      p->stats.bytes_moved += gate_algorithmic_bytes(n, P.gates[0]);
+      p->passes.push_back(pp);
+      continue;
+    }
+    PassArgs& A = pp.args;
+    A.k = (int)P.local.size();
+    A.c = c;
+    A.nhigh = A.k - c;
+    for (int j = 0; j < A.k; ++j) A.lpos[j] = (uint8_t)P.local[j];
+    A.ntiles = 1ull << (n - A.k);
+    A.gates = (const TileGate*)p->dbuf + offs[q];
+    A.tables = (const double2*)((char*)p->dbuf + gbytes);
+    A.ngates = (int)P.gates.size();
+    const uint32_t T = 1u << A.k;
+    pp.smem = 2 * T * sizeof(double) + (size_t)(1u << A.nhigh) * sizeof(uint64_t);
+    pp.threads = (int)std::min<uint32_t>(kTileThreads, std::max<uint32_t>(32, T / 2));
+    int resident = 0, sms = 0;
+    int rc = tile_launch_shape(p->device, pp.threads, pp.smem, &resident, &sms);
+    if (rc) return rc;
+    pp.blocks = std::min<uint64_t>(A.ntiles, (uint64_t)sms * resident);
+    p->stats.tile_passes++;
+    p->stats.bytes_moved += 32ull << n;
+    p->passes.push_back(pp);
+  }
+  return SPZ_OK;
+}
+
+// Capture the program's launches for state h (on the private stream).
+int capture_program(spz_program_t p, spz_state_t h) {
+  if (!p->capture) SPZ_CUDA(cudaStreamCreateWithFlags(&p->capture, cudaStreamNonBlocking));
+  spz_state_s v;  // h's arrays, launched on the capture stream
+  v.n = h->n;
+  v.N = h->N;
+  v.re = h->re;
+  v.im = h->im;
+  v.owns = false;
+  v.stream = p->capture;
+  v.device = h->device;
+  SPZ_CUDA(cudaStreamBeginCapture(p->capture, cudaStreamCaptureModeThreadLocal));
+  int rc = SPZ_OK;
+  for (const ProgramPass& pp : p->passes) {
+    if (!pp.tiled) {
+      rc = launch_gate(&v, pp.plain);
+    } else {
+      PassArgs A = pp.args;
+      A.re = h->re;
+      A.im = h->im;
+      A.outcomes = nullptr;
+      tile_kernel<<<(unsigned)pp.blocks, pp.threads, pp.smem, p->capture>>>(A);
+      cudaError_t le = cudaGetLastError();
+      if (le != cudaSuccess) rc = cuda_fail(le, "tile_kernel");
+    }
+    if (rc) break;
+  }
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamEndCapture(p->capture, &g);
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "program graph capture");
+  if (p->exec) {
+    cudaGraphExecDestroy(p->exec);
+    p->exec = nullptr;
+  }
+  e = cudaGraphInstantiate(&p->exec, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return cuda_fail(e, "program graph instantiation");
+  p->exec_re = h->re;
+  p->exec_im = h->im;
+  return SPZ_OK;
+}
+
+}  // namespace
+
 }  // namespace spz
 
 using namespace spz;
@@ -1149,6 +1355,46 @@ int spz_iqft(spz_state_t h, const uint32_t* targets, uint32_t ntargets) {
     }
   }
   return execute(h, ops.data(), ops.size(), nullptr, SPZ_EXEC_DEFAULT, nullptr);
+}
+
+int spz_program_create(uint32_t n, const spz_op* ops, size_t nops, uint32_t flags, spz_program_t* out) {
+  if (!out || (nops && !ops)) return fail(SPZ_ERR_NULL, "NULL argument");
+  if (n == 0 || n > kMaxQubits) return fail(SPZ_ERR_INVALID_ARGUMENT, "n out of range");
+  spz_program_t p = new (std::nothrow) spz_program_s();
+  if (!p) return fail(SPZ_ERR_OUT_OF_MEMORY, "host allocation failed");
+  p->n = n;
+  cudaError_t e = cudaGetDevice(&p->device);
+  int rc = e == cudaSuccess ? build_program(p, ops, nops, flags) : cuda_fail(e, "cudaGetDevice");
+  if (rc) {
+    free_program(p);
+    return rc;
+  }
+  *out = p;
+  return SPZ_OK;
+}
+
+int spz_program_run(spz_program_t p, spz_state_t h) {
+  if (!p || !h) return fail(SPZ_ERR_NULL, "NULL argument");
+  if (h->n != p->n) return fail(SPZ_ERR_INVALID_ARGUMENT, "the state's qubit count differs from the program's");
+  if (p->passes.empty()) return SPZ_OK;
+  if (!p->exec || p->exec_re != h->re || p->exec_im != h->im) {
+    int rc = capture_program(p, h);
+    if (rc) return rc;
+  }
+  SPZ_CUDA(cudaGraphLaunch(p->exec, h->stream));
+  return SPZ_OK;
+}
+
+int spz_program_stats(spz_program_t p, spz_exec_stats* stats) {
+  if (!p || !stats) return fail(SPZ_ERR_NULL, "NULL argument");
+  *stats = p->stats;
+  return SPZ_OK;
+}
+
+int spz_program_destroy(spz_program_t p) {
+  if (p && p->capture) cudaStreamSynchronize(p->capture);
+  free_program(p);
+  return SPZ_OK;
 }
 
 }  // extern "C"

@@ -396,3 +396,63 @@ def test_execute_host_reuses_a_state_and_checks_sizes(gpu):
     assert np.array_equal(re, want[0]) and np.array_equal(im, want[1])
     with pytest.raises(ValueError):
         circuit.execute_host(ops, np.zeros(1 << (n + 1)), np.zeros(1 << (n + 1)), state=s)
+
+
+# ---------------------------------------------------------------- programs
+@pytest.mark.parametrize("mode", ["fused", "fast", "unfused"])
+def test_program_replays_equal_execute(gpu, mode):
+    """A compiled program (planned once, replayed as a CUDA graph) gives what
+    spz_circuit_execute gives, run after run, on one state or another."""
+    import torch
+
+    n = 13
+    ops = random_circuit(n, 150, 7)
+    init = rng.normal_state(n, 41)
+    fused, fast = mode != "unfused", mode == "fast"
+    prog = circuit.Program(n, ops, fused=fused, fast=fast)
+    s = State.from_arrays(*init)
+    want = State.from_arrays(*init)
+    ref = QuantumCircuit.from_state(want, fused=fused, fast=fast)
+    for _ in range(3):  # capture, then two replays
+        prog.run(s)
+        ref.execute_ops(ops)
+        s.synchronize()
+        a, b = s.to_numpy(), want.to_numpy()
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    other = State.from_arrays(*init)  # a different state: captured again
+    prog.run(other)
+    other.synchronize()
+    o = other.to_numpy()
+    first, _, _ = _run_gpu(n, ops, init, fused=fused)
+    if not fast:
+        assert np.array_equal(o[0], first[0]) and np.array_equal(o[1], first[1])
+    st = prog.stats()
+    assert st["gates"] == len(ops) and st["passes"] >= 1
+    prog.close()
+    _ = torch
+
+
+def test_program_on_torch_stream_and_rejects_measurements(gpu):
+    import torch
+
+    n = 12
+    ops = brickwork(n, 3)
+    re = torch.zeros(1 << n, dtype=torch.float64, device="cuda")
+    im = torch.zeros(1 << n, dtype=torch.float64, device="cuda")
+    re[0] = 1.0
+    s = State.from_torch(re, im)
+    s.set_stream(torch.cuda.current_stream())
+    prog = circuit.Program(n, ops)
+    prog.run(s)
+    torch.cuda.synchronize()
+    e0 = np.zeros(1 << n)
+    e0[0] = 1.0
+    want, _, _ = _run_gpu(n, ops, (e0, np.zeros(1 << n)))
+    assert np.array_equal(re.cpu().numpy(), want[0]) and np.array_equal(im.cpu().numpy(), want[1])
+    qc = _builder()
+    qc.h(0)
+    qc.measure(0)
+    with pytest.raises(NotImplementedError):
+        circuit.Program(n, qc.ops())
+    with pytest.raises(ValueError):
+        prog.run(State(n + 1))
