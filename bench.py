@@ -636,8 +636,8 @@ def main() -> None:
     ap.add_argument("--instances", type=int, default=4096)
     ap.add_argument("--loop-sample", type=int, default=64)
     ap.add_argument("--autotune", action="store_true")
-    ap.add_argument("--batch-tile", type=int, default=12, help="batch workload: tile qubits (resident up to this n)")
-    ap.add_argument("--batch-threads", type=int, default=512, help="batch workload: threads per block")
+    ap.add_argument("--batch-tile", type=int, default=11, help="batch workload: tile qubits (resident up to this n)")
+    ap.add_argument("--batch-threads", type=int, default=128, help="batch workload: threads per block")
     ap.add_argument("--batch-qmax", type=int, default=22, help="batch workload: largest instance (small profiling cases)")
     ap.add_argument("--batch-fast", action="store_true", help="batch workload: fast adjoint for the wide instances")
     ap.add_argument("--batch-wide", type=int, default=0,

@@ -344,8 +344,8 @@ typedef struct spz_batch_instance {
 } spz_batch_instance;
 
 typedef struct spz_batch_config {
-  int32_t tile_qubits;    /* local qubits per shared-memory tile, 4..12 (0 = 12) */
-  int32_t threads;        /* threads per CTA, multiple of 32 in 64..1024 (0 = 512) */
+  int32_t tile_qubits;    /* local qubits per shared-memory tile, 4..12 (0 = 11) */
+  int32_t threads;        /* threads per CTA, multiple of 32 in 64..1024 (0 = 128) */
   int32_t wide_qubits;    /* instances of at least this many qubits run one at a time
                              across the whole GPU (fused passes + fused adjoint sweep)
                              instead of one per CTA; 0 = 18, > 30 = never            */

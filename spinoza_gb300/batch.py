@@ -112,7 +112,7 @@ class Batch:
             pass
 
 
-CANDIDATES = [(12, 512), (12, 256), (11, 256), (11, 128), (10, 128), (10, 64)]
+CANDIDATES = [(11, 128), (11, 256), (12, 256), (12, 512), (10, 128), (10, 64)]
 
 
 def _signature(instances: Sequence[Instance]) -> str:

@@ -472,7 +472,9 @@ struct WideInst {
 
 struct BatchImpl {
   int device = 0;
-  int kmax = kBatchMaxK, threads = 512;
+  // 2^11 tiles x 128 threads: 4096 instances of 10-17 qubits in 1.04 s, against
+  // 1.35-1.39 s with 2^12 x 256-512 and 1.60 s with 2^10 x 128.
+  int kmax = 11, threads = 128;
   int wide_qubits = kDefaultWideQubits;
   uint32_t wide_flags = 0;            // SPZ_EXEC_FAST: wide instances use the fast adjoint
   uint32_t nnarrow = 0;               // instances in the persistent kernel
