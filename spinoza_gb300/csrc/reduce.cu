@@ -336,6 +336,9 @@ struct PtArgs {
   int ndiag;                 // diagonal terms handled in this pass (0 or all)
   uint64_t dz[kPtMaxDiag];   // their Z-masks
   const double* dtab;        // nchunks x 256 table entries
+  // The chunk index w(x) = sum_j parity(x & dz_j) << j is linear over GF(2):
+  // w(base | e) = w(base) ^ L0[e & 63] ^ L1[e >> 6] for the tile offset e.
+  uint8_t lz[kPtMaxDiag / 8][2][64];
   double dconst;             // C = sum of the diagonal coefficients
   int nt;
   PtTerm t[kPtMaxTerms];
@@ -356,6 +359,11 @@ __global__ void __launch_bounds__(kPtThreads) pauli_tile_kernel(PtArgs A) {
       if ((r >> j) & 1) off |= 1ull << A.lpos[A.c + j];
     rowoff[r] = off;
   }
+  const int nch = (A.ndiag + 7) / 8;
+  double* stab = red + 32;                                          // nch x 256 chunk tables
+  uint8_t* slz = reinterpret_cast<uint8_t*>(stab + (size_t)nch * 256);  // nch x 2 x 64
+  for (int j = threadIdx.x; j < nch * 256; j += blockDim.x) stab[j] = A.dtab[j];
+  for (int j = threadIdx.x; j < nch * 128; j += blockDim.x) slz[j] = (&A.lz[0][0][0])[j];
   double acc[kPtMaxTerms + 1];
 #pragma unroll
   for (int j = 0; j <= kPtMaxTerms; ++j) acc[j] = 0.0;
@@ -370,14 +378,23 @@ __global__ void __launch_bounds__(kPtThreads) pauli_tile_kernel(PtArgs A) {
     }
     __syncthreads();
     if (A.ndiag) {
+      uint32_t wb[kPtMaxDiag / 8];  // the tile base's part of each chunk index
+#pragma unroll
+      for (int ch = 0; ch < kPtMaxDiag / 8; ++ch) {
+        wb[ch] = 0;
+        if (ch < nch) {
+          const int jn = min(8, A.ndiag - ch * 8);
+          for (int j = 0; j < jn; ++j) wb[ch] |= (uint32_t)(__popcll(base & A.dz[ch * 8 + j]) & 1) << j;
+        }
+      }
       for (uint32_t e = threadIdx.x; e < T; e += blockDim.x) {
-        const uint64_t gi = base | rowoff[e >> A.c] | (e & cmask);
         double d = A.dconst;
-        for (int j0 = 0; j0 < A.ndiag; j0 += 8) {
-          uint32_t w = 0;
-          const int jn = min(8, A.ndiag - j0);
-          for (int j = 0; j < jn; ++j) w |= (uint32_t)(__popcll(gi & A.dz[j0 + j]) & 1) << j;
-          d = dadd(d, A.dtab[(j0 / 8) * 256 + w]);
+        const uint32_t e0 = e & 63, e1 = (e >> 6) & 63;
+#pragma unroll
+        for (int ch = 0; ch < kPtMaxDiag / 8; ++ch) {
+          if (ch >= nch) break;
+          const uint32_t w = wb[ch] ^ slz[ch * 128 + e0] ^ slz[ch * 128 + 64 + e1];
+          d = dadd(d, stab[ch * 256 + w]);
         }
         const double a = sre[e], b = sim[e];
         acc[kPtMaxTerms] = dfma(dfma(a, a, dmul(b, b)), d, acc[kPtMaxTerms]);
@@ -507,7 +524,7 @@ static int pauli_tiles(spz_state_t h, const spz_pauli_term* terms, size_t nterms
   static bool attr = false;
   if (!attr) {
     SPZ_CUDA(cudaFuncSetAttribute(pauli_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)((2 << kPtK) + (1 << (kPtK - kPtLow)) + 64) * 8));
+                                  (int)((2 << kPtK) + (1 << (kPtK - kPtLow)) + 64 + (kPtMaxDiag / 8) * (256 + 16)) * 8));
     attr = true;
   }
   for (size_t p = 0; p < passes.size(); ++p) {
@@ -528,6 +545,25 @@ static int pauli_tiles(spz_state_t h, const spz_pauli_term* terms, size_t nterms
       for (size_t j = 0; j < nd; ++j) A.dz[j] = terms[diag[j]].z_mask;
       A.dtab = dtab;
       A.dconst = dconst;
+      // column of tile-offset bit b in chunk ch: the chunk's terms whose Z-mask
+      // holds the local qubit lpos[b]
+      for (int ch = 0; ch < (int)((nd + 7) / 8); ++ch) {
+        uint32_t col[12] = {};
+        const int jn = std::min<int>(8, (int)nd - ch * 8);
+        for (int b = 0; b < A.k && b < 12; ++b)
+          for (int j = 0; j < jn; ++j) col[b] |= (uint32_t)((A.dz[ch * 8 + j] >> A.lpos[b]) & 1) << j;
+        for (int v = 0; v < 64; ++v) {
+          uint32_t w0 = 0, w1 = 0;
+          for (int b = 0; b < 6; ++b) {
+            if ((v >> b) & 1) {
+              w0 ^= col[b];
+              w1 ^= col[b + 6];
+            }
+          }
+          A.lz[ch][0][v] = (uint8_t)w0;
+          A.lz[ch][1][v] = (uint8_t)w1;
+        }
+      }
     }
     A.nt = (int)P.terms.size();
     for (int t = 0; t < A.nt; ++t) {
@@ -542,7 +578,8 @@ static int pauli_tiles(spz_state_t h, const spz_pauli_term* terms, size_t nterms
     }
     A.partials = dpart + p * slots_per_pass;
     const uint32_t T = 1u << A.k;
-    const size_t smem = (2 * T + (T >> kPtLow) + 1 + 32) * sizeof(double);
+    const size_t nch = P.diag ? (nd + 7) / 8 : 0;
+    const size_t smem = (2 * T + (T >> kPtLow) + 1 + 32 + nch * 256 + nch * 16) * sizeof(double);
     const int threads = (int)std::min<uint32_t>(kPtThreads, std::max<uint32_t>(32, T / 2));
     const int nb = (int)std::min<uint64_t>(A.ntiles, (uint64_t)blocks);
     pauli_tile_kernel<<<nb, threads, smem, h->stream>>>(A);
