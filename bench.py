@@ -511,14 +511,16 @@ def workload_qft20(args) -> None:
     d_fast = float(max(np.max(np.abs(gre - re)), np.max(np.abs(gim - im))))
     d = float(max(np.max(np.abs(pre - re)), np.max(np.abs(pim - im))))
     abytes = algorithmic_bytes(ops, n)
-    _line("config1 QFT-20 circuit time", out["fused"] * 1e3, "ms", args, higher_is_better=False,
+    _line("config1 QFT-20 circuit time", out["program_fast"] * 1e3, "ms", args, higher_is_better=False,
           config={"workload": "QFT with swaps, 20 qubits, N(0,1) normalised state seed 1", "gates": len(ops)},
-          unfused_ms=out["unfused"] * 1e3, effective_gbs=abytes / out["fused"] / 1e9,
+          execute_ms=out["fused"] * 1e3, unfused_ms=out["unfused"] * 1e3,
+          effective_gbs=abytes / out["program_fast"] / 1e9,
           passes=circuit.plan_stats(n, ops)["passes"], cpu_baseline_ms=t_cpu * 1e3, cpu_threads=oracle.num_threads(),
           program_ms=out["program"] * 1e3, program_fast_ms=out["program_fast"] * 1e3,
           max_abs_diff_vs_oracle=d, bit_identical=bool(d == 0.0), max_abs_diff_fast_vs_oracle=d_fast,
-          note="value: spz_circuit_execute per run (plans each time); program_*: planned once, replayed as a "
-               "CUDA graph; each run includes a device copy of the input state")
+          note="value: the fast-mode program (planned once, replayed as a CUDA graph); execute_ms: the bit-exact "
+               "spz_circuit_execute (plans each run); program_ms: the bit-exact program; every run includes a "
+               "device copy of the input state")
 
 
 def workload_measure28(args) -> None:

@@ -9,7 +9,9 @@
 //     the remaining coefficient has magnitude <= 1); the scalars multiply into
 //     one global factor G.  4 FP64 instructions per pair instead of 8-12.
 //   * U(theta, phi, lambda) = P(phi) RY(theta) P(lambda); RZ(theta) =
-//     e^{-i theta/2} P(theta); Z = P(pi); Y = i X Z.
+//     e^{-i theta/2} P(theta); Z = P(pi); Y = i X Z; a diagonal gate with one
+//     control (CZ, CP, CRZ) is x_c (b0 + a x_t) in the phase, i.e. three
+//     parity terms ({c}, {t}, {c, t}), since x_c x_t = (x_c + x_t - x_c^x_t)/2.
 //   * single-qubit phases are not applied where they occur: they are kept as
 //     pending terms e^{i alpha parity(x & S)} and pushed through the
 //     permutations that follow (X flips alpha and multiplies G by e^{i alpha};
@@ -255,7 +257,26 @@ struct Lowering {
           }
         }
       }
-      emit(g);  // controlled diagonal: commutes with the pending terms
+      if (g.zeros == 0 && __builtin_popcountll(g.ones) == 1) {
+        // One control c: the phase is x_c (b0 + a x_t), and
+        // x_c x_t = (x_c + x_t - (x_c xor x_t)) / 2, so three parity terms.
+        const int cq = __builtin_ctzll(g.ones);
+        double b0 = 0.0, a;
+        switch (g.kind) {
+          case SPZ_GATE_Z: a = kPiF; break;
+          case SPZ_GATE_P: a = std::atan2(g.c.sn, g.c.cs); break;
+          default: {  // RZ: d0 on x_t = 0, d1 on x_t = 1 (both of modulus 1)
+            const std::complex<double> d0(g.c.d0re, g.c.d0im), d1(g.c.d1re, g.c.d1im);
+            b0 = std::arg(d0);
+            a = std::arg(d1 / d0);
+          }
+        }
+        add_term(1ull << cq, b0 + 0.5 * a);
+        add_term(1ull << q, 0.5 * a);
+        add_term((1ull << cq) | (1ull << q), -0.5 * a);
+        return;
+      }
+      emit(g);  // other controlled diagonals: they commute with the pending terms
       return;
     }
     if (controls == 0) {
