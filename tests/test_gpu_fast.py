@@ -1,6 +1,6 @@
 """Fast mode (SPZ_EXEC_FAST) vs the oracle: the same circuits, rewritten to
 need fewer FP64 instructions (lazy scaling, U = P RY P, phases pushed through
-permutations).  Not bit-identical by design; the bound is the north-star
+permutations).  Not bit-identical by design; the bound is the parity bound of
 1e-12 on every amplitude (states here have |amplitude| <= 1)."""
 import math
 
