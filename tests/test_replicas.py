@@ -29,7 +29,7 @@ def _rank_main(rank, world, port, out):
 
 def test_two_replicas_take_the_max_time_and_sum_the_work():
     port = 29500 + (os.getpid() % 1000)
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:
         out = m.dict()
         mp.spawn(_rank_main, args=(2, port, out), nprocs=2, join=True)
         res = dict(out)
