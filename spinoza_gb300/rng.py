@@ -28,6 +28,21 @@ def u64(seed: int, start: int, count: int) -> np.ndarray:
         return _mix(key + idx * GOLDEN)
 
 
+def u64_at(seed: int, idx: np.ndarray) -> np.ndarray:
+    """The 64-bit values of stream `seed` at arbitrary counter positions `idx`."""
+    with np.errstate(over="ignore"):
+        key = _mix(np.array([seed], dtype=np.uint64) + GOLDEN)[0]
+        return _mix(key + (np.asarray(idx, dtype=np.uint64) + np.uint64(1)) * GOLDEN)
+
+
+def uniform_amplitudes(seed: int, idx: np.ndarray) -> tuple[np.ndarray, np.ndarray]:
+    """Amplitudes `idx` of uniform_state(n, seed) for any n, without the rest of the state."""
+    i2 = np.asarray(idx, dtype=np.uint64) * np.uint64(2)
+    ure = (u64_at(seed, i2) >> np.uint64(11)).astype(np.float64) * (2.0 ** -53)
+    uim = (u64_at(seed, i2 + np.uint64(1)) >> np.uint64(11)).astype(np.float64) * (2.0 ** -53)
+    return 2.0 * ure - 1.0, 2.0 * uim - 1.0
+
+
 def uniforms(seed: int, count: int, start: int = 0) -> np.ndarray:
     """count uniforms in [0, 1) with 53 random bits each."""
     return (u64(seed, start, count) >> np.uint64(11)).astype(np.float64) * (2.0 ** -53)

@@ -56,6 +56,17 @@ def test_uniform_state_matches_oracle():
     assert np.array_equal(re, ore) and np.array_equal(im, oim)
 
 
+def test_uniform_amplitudes_regenerate_any_index():
+    re, im = rng.uniform_state(12, 31)
+    idx = np.array([0, 1, 7, 4095, 2048, 1234, 7], dtype=np.uint64)
+    gre, gim = rng.uniform_amplitudes(31, idx)
+    assert np.array_equal(gre, re[idx.astype(np.int64)]) and np.array_equal(gim, im[idx.astype(np.int64)])
+    # an index far beyond any state held on the host (bit 40 set)
+    big = np.array([(1 << 40) + 5], dtype=np.uint64)
+    bre, _ = rng.uniform_amplitudes(31, big)
+    assert bre[0] == 2.0 * oracle.stream_uniform(31, 2 * ((1 << 40) + 5)) - 1.0
+
+
 def test_normal_state_is_normalised():
     re, im = rng.normal_state(12, 1)
     assert abs(np.sum(re * re + im * im) - 1.0) < 1e-12
