@@ -240,7 +240,7 @@ __device__ __forceinline__ double adj_diag_any(const TileGate& g, int mode, int 
   return r;
 }
 
-__global__ void __launch_bounds__(kAdjTileThreads) adj_tile_kernel(AdjPassArgs A) {
+__global__ void __launch_bounds__(kAdjTileThreads) adj_tile_kernel(const __grid_constant__ AdjPassArgs A) {
   extern __shared__ double sm[];
   const int K = A.k;
   const uint32_t T = 1u << K;
@@ -252,16 +252,12 @@ __global__ void __launch_bounds__(kAdjTileThreads) adj_tile_kernel(AdjPassArgs A
   double* wacc = reinterpret_cast<double*>(rowoff + (1u << A.nhigh));  // [kAdjWarps][kAdjMaxSlots]
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t cmask = (1u << A.c) - 1;
-  for (uint32_t r = threadIdx.x; r < (1u << A.nhigh); r += blockDim.x) {
-    uint64_t off = 0;
-    for (int j = 0; j < A.nhigh; ++j)
-      if ((r >> j) & 1) off |= 1ull << A.lpos[A.c + j];
-    rowoff[r] = off;
-  }
+  for (uint32_t r = threadIdx.x; r < (1u << A.nhigh); r += blockDim.x)
+    rowoff[r] = row_offset_param<kAdjTileK>(r, A.lpos, A.c, K);
   for (int j = threadIdx.x; j < kAdjWarps * kAdjMaxSlots; j += blockDim.x) wacc[j] = 0.0;
   __syncthreads();
   for (uint64_t tile = blockIdx.x; tile < A.ntiles; tile += gridDim.x) {
-    const uint64_t base = deposit(tile, A.lpos, K);
+    const uint64_t base = deposit_param<kAdjTileK>(tile, A.lpos, K);
     for (uint32_t e2 = threadIdx.x; e2 < T / 2; e2 += blockDim.x) {
       const uint32_t e = 2 * e2;
       const uint64_t gi = base | rowoff[e >> A.c] | (e & cmask);

@@ -163,6 +163,11 @@ __global__ void __launch_bounds__(kTileThreads, SPZ_TILE_MIN_BLOCKS) tile_kernel
   const uint32_t nrows = 1u << A.nhigh;
   const uint32_t cmask = (1u << A.c) - 1;
   // Row offsets: scatter of the high local bits, the same for every tile.
+  // (The run-time index into A.lpos here and in deposit() keeps the parameter
+  // block in local memory.  Reading lpos at constant indices instead
+  // (deposit_param) removes it but measured 1.9% slower on the 30-qubit
+  // brickwork, in fast mode, and no faster in the exact mode; the adjoint
+  // kernel, where it measured 1.3% faster, uses that form.)
   for (uint32_t r = threadIdx.x; r < nrows; r += blockDim.x) {
     uint64_t off = 0;
     for (int j = 0; j < A.nhigh; ++j)

@@ -103,6 +103,32 @@ __device__ __forceinline__ uint64_t deposit(uint64_t k, const uint8_t* pos, int 
   return k;
 }
 
+// deposit() for positions held in a kernel parameter: pos[] is read at
+// constant indices only (j < MAXK, unrolled).  A run-time index into a
+// by-value kernel parameter makes the compiler copy the whole parameter block
+// to local memory, after which every read of it is a local load.
+template <int MAXK>
+__device__ __forceinline__ uint64_t deposit_param(uint64_t k, const uint8_t* pos, int npos) {
+#pragma unroll
+  for (int j = 0; j < MAXK; ++j) {
+    if (j < npos) {
+      const uint64_t p = pos[j];
+      k = ((k >> p) << (p + 1)) | (k & ((1ull << p) - 1));
+    }
+  }
+  return k;
+}
+
+// Offset of row r of a tile: bit j of r scattered to position pos[c + j].
+template <int MAXK>
+__device__ __forceinline__ uint64_t row_offset_param(uint32_t r, const uint8_t* pos, int c, int k) {
+  uint64_t off = 0;
+#pragma unroll
+  for (int j = 0; j < MAXK; ++j)
+    if (j >= c && j < k && ((r >> (j - c)) & 1)) off |= 1ull << pos[j];
+  return off;
+}
+
 // ------------------------------------------------------ gate coefficients
 // Host-computed coefficients, exactly as the reference computes them
 // (glibc sin/cos, the same sub-expressions); see coef_for() in gates.cu.
