@@ -75,20 +75,54 @@ __device__ __forceinline__ void tile_fast_phase(const TileGate& g, const double2
     bidx |= (uint32_t)(__popcll(base & g.pmask[j]) & 1) << j;
     em[j] = g.pemask[j];
   }
-#pragma unroll kTileUnroll
-  for (uint32_t m = threadIdx.x; m < npairs; m += blockDim.x) {
-    const uint32_t e0 = E(m);
-    const uint32_t s0 = TileSwizzle::at(e0), s1 = TileSwizzle::at(e0 | tbit);
-    uint32_t idx = bidx;
+  if constexpr (kTileBatch > 1) {  // see tile_pair
+    const uint32_t step = blockDim.x;
+    for (uint32_t m0 = threadIdx.x; m0 < npairs; m0 += kTileBatch * step) {
+      uint32_t s0[kTileBatch], s1[kTileBatch];
+      double a[kTileBatch], b[kTileBatch], x[kTileBatch], d[kTileBatch];
+      double2 w[kTileBatch];
 #pragma unroll
-    for (int j = 0; j < PM; ++j) idx ^= (uint32_t)(__popc(e0 & em[j]) & 1) << j;
-    const double2 w = __ldg(tab + idx);
-    double a = sre[s0], b = sim[s0];
-    const double r = sre[s1], i = sim[s1];
-    double x = dfma(r, w.x, dmul(dneg(i), w.y));
-    double d = dfma(r, w.y, dmul(i, w.x));
-    fast_pair<FK>(c, a, b, x, d);
-    sre[s0] = a; sim[s0] = b; sre[s1] = x; sim[s1] = d;
+      for (int u = 0; u < kTileBatch; ++u) {
+        const uint32_t m = m0 + u * step;
+        const uint32_t e0 = E(m < npairs ? m : m0);
+        s0[u] = TileSwizzle::at(e0);
+        s1[u] = TileSwizzle::at(e0 | tbit);
+        uint32_t idx = bidx;
+#pragma unroll
+        for (int j = 0; j < PM; ++j) idx ^= (uint32_t)(__popc(e0 & em[j]) & 1) << j;
+        w[u] = __ldg(tab + idx);
+        a[u] = sre[s0[u]]; b[u] = sim[s0[u]]; x[u] = sre[s1[u]]; d[u] = sim[s1[u]];
+      }
+#pragma unroll
+      for (int u = 0; u < kTileBatch; ++u) {
+        const double r = x[u], i = d[u];
+        x[u] = dfma(r, w[u].x, dmul(dneg(i), w[u].y));
+        d[u] = dfma(r, w[u].y, dmul(i, w[u].x));
+        fast_pair<FK>(c, a[u], b[u], x[u], d[u]);
+      }
+#pragma unroll
+      for (int u = 0; u < kTileBatch; ++u) {
+        if (m0 + u * step < npairs) {
+          sre[s0[u]] = a[u]; sim[s0[u]] = b[u]; sre[s1[u]] = x[u]; sim[s1[u]] = d[u];
+        }
+      }
+    }
+  } else {
+#pragma unroll kTileUnroll
+    for (uint32_t m = threadIdx.x; m < npairs; m += blockDim.x) {
+      const uint32_t e0 = E(m);
+      const uint32_t s0 = TileSwizzle::at(e0), s1 = TileSwizzle::at(e0 | tbit);
+      uint32_t idx = bidx;
+#pragma unroll
+      for (int j = 0; j < PM; ++j) idx ^= (uint32_t)(__popc(e0 & em[j]) & 1) << j;
+      const double2 w = __ldg(tab + idx);
+      double a = sre[s0], b = sim[s0];
+      const double r = sre[s1], i = sim[s1];
+      double x = dfma(r, w.x, dmul(dneg(i), w.y));
+      double d = dfma(r, w.y, dmul(i, w.x));
+      fast_pair<FK>(c, a, b, x, d);
+      sre[s0] = a; sim[s0] = b; sre[s1] = x; sim[s1] = d;
+    }
   }
 }
 

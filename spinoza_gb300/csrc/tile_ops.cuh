@@ -79,19 +79,57 @@ constexpr int kTileUnroll = SPZ_TILE_UNROLL;
     default: CALL(-1); break;   \
   }
 
+// Pairs handled per loop iteration and thread.  The pairs of one op are
+// disjoint, but the compiler cannot prove that the next pair's shared-memory
+// loads do not alias this pair's stores, so unrolling alone cannot overlap
+// them; the batched loop loads kTileBatch pairs, computes them, then stores.
+// Measured on the 30-qubit brickwork with 2: fast mode 4% slower (80
+// registers instead of 72), exact mode 0.7% faster; 4 spills.  So 1.
+#ifndef SPZ_TILE_BATCH
+#define SPZ_TILE_BATCH 1
+#endif
+constexpr int kTileBatch = SPZ_TILE_BATCH;
+
 template <int KIND, int NPOS, class G, class SW = NoSwizzle>
 __device__ __forceinline__ void tile_pair(const G& g, double* sre, double* sim, uint32_t npairs) {
   const Enumerator<NPOS, G> E(g);
   const uint32_t tbit = g.tbit;
   const Coef c = g.c;
+  if constexpr (kTileBatch > 1) {
+    const uint32_t step = blockDim.x;
+    for (uint32_t m0 = threadIdx.x; m0 < npairs; m0 += kTileBatch * step) {
+      uint32_t s0[kTileBatch], s1[kTileBatch];
+      double a[kTileBatch], b[kTileBatch], x[kTileBatch], d[kTileBatch];
+#pragma unroll
+      for (int u = 0; u < kTileBatch; ++u) {
+        const uint32_t m = m0 + u * step;
+        const uint32_t e0 = E(m < npairs ? m : m0);
+        s0[u] = SW::at(e0);
+        s1[u] = SW::at(e0 | tbit);
+        a[u] = sre[s0[u]]; b[u] = sim[s0[u]]; x[u] = sre[s1[u]]; d[u] = sim[s1[u]];
+      }
+#pragma unroll
+      for (int u = 0; u < kTileBatch; ++u) {
+        if constexpr (KIND >= FK_LAZY_H) fast_pair<KIND>(c, a[u], b[u], x[u], d[u]);
+        else gate_pair<KIND>(c, a[u], b[u], x[u], d[u]);
+      }
+#pragma unroll
+      for (int u = 0; u < kTileBatch; ++u) {
+        if (m0 + u * step < npairs) {
+          sre[s0[u]] = a[u]; sim[s0[u]] = b[u]; sre[s1[u]] = x[u]; sim[s1[u]] = d[u];
+        }
+      }
+    }
+  } else {
 #pragma unroll kTileUnroll
-  for (uint32_t m = threadIdx.x; m < npairs; m += blockDim.x) {
-    const uint32_t e0 = E(m);
-    const uint32_t s0 = SW::at(e0), s1 = SW::at(e0 | tbit);
-    double a = sre[s0], b = sim[s0], x = sre[s1], d = sim[s1];
-    if constexpr (KIND >= FK_LAZY_H) fast_pair<KIND>(c, a, b, x, d);
-    else gate_pair<KIND>(c, a, b, x, d);
-    sre[s0] = a; sim[s0] = b; sre[s1] = x; sim[s1] = d;
+    for (uint32_t m = threadIdx.x; m < npairs; m += blockDim.x) {
+      const uint32_t e0 = E(m);
+      const uint32_t s0 = SW::at(e0), s1 = SW::at(e0 | tbit);
+      double a = sre[s0], b = sim[s0], x = sre[s1], d = sim[s1];
+      if constexpr (KIND >= FK_LAZY_H) fast_pair<KIND>(c, a, b, x, d);
+      else gate_pair<KIND>(c, a, b, x, d);
+      sre[s0] = a; sim[s0] = b; sre[s1] = x; sim[s1] = d;
+    }
   }
 }
 
