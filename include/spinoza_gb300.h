@@ -11,7 +11,10 @@
  *     exactly the layout of `State { reals, imags, n }` (spinoza/src/core.rs:20-27).
  *   - A handle owns (or wraps) the two device arrays and one CUDA stream.  All
  *     work on a handle is issued on that stream; calls on one handle must be
- *     serialised by the caller (the reference borrows `&mut State`).
+ *     serialised by the caller (the reference borrows `&mut State`).  A handle
+ *     belongs to the device that was current when it was created; make that
+ *     device current (cudaSetDevice) before calls on it.  Handles on different
+ *     devices or threads may be used concurrently.
  *   - Every function returns an int status (SPZ_OK == 0).  Nothing throws across
  *     the ABI.  Where the reference panics (bad qubit index, unsupported gate,
  *     n == 0) this library returns an error code and leaves the state untouched.

@@ -599,15 +599,27 @@ int adjoint_gradient(spz_state_t h, const spz_op* ops, size_t nops, const uint32
   // Launch shape: one wave of resident blocks.
   const uint32_t T = 1u << k;
   const size_t smem = (4 * (size_t)T + (size_t)(1u << (k - c)) + (size_t)kAdjWarps * kAdjMaxSlots) * sizeof(double);
-  static int resident = 0, sms = kNumSMs;
-  if (!resident) {
-    SPZ_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, h->device));
-    const size_t max_smem = (4 * ((size_t)1 << kAdjTileK) + ((size_t)1 << (kAdjTileK - kTileLowBits)) +
-                             (size_t)kAdjWarps * kAdjMaxSlots) * sizeof(double);
-    SPZ_CUDA(cudaFuncSetAttribute(adj_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem));
-    int per_sm = 0;
-    SPZ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, adj_tile_kernel, kAdjTileThreads, max_smem));
-    resident = std::max(1, per_sm);
+  // Resident blocks per SM and the SM count, set up once per device (kernel
+  // attributes are per device; first calls may come from several threads).
+  static std::mutex shape_mu;
+  static int shape_resident[kMaxDevices] = {}, shape_sms[kMaxDevices] = {};
+  if (h->device < 0 || h->device >= kMaxDevices) return fail(SPZ_ERR_INVALID_ARGUMENT, "device index out of range");
+  int resident = 0, sms = 0;
+  {
+    std::lock_guard<std::mutex> lock(shape_mu);
+    if (!shape_resident[h->device]) {
+      int count = 0;
+      SPZ_CUDA(cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount, h->device));
+      const size_t max_smem = (4 * ((size_t)1 << kAdjTileK) + ((size_t)1 << (kAdjTileK - kTileLowBits)) +
+                               (size_t)kAdjWarps * kAdjMaxSlots) * sizeof(double);
+      SPZ_CUDA(cudaFuncSetAttribute(adj_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)max_smem));
+      int per_sm = 0;
+      SPZ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, adj_tile_kernel, kAdjTileThreads, max_smem));
+      shape_sms[h->device] = count;
+      shape_resident[h->device] = std::max(1, per_sm);
+    }
+    resident = shape_resident[h->device];
+    sms = shape_sms[h->device];
   }
   const uint64_t ntiles = 1ull << (n - k);
   const int blocks = (int)std::min<uint64_t>(ntiles, (uint64_t)sms * resident);

@@ -552,27 +552,33 @@ uint64_t op_fp64_ops(uint32_t n, const GateApp& g, const std::vector<PhaseTable>
 
 // Resident blocks per SM for a tile pass of `threads` x `smem` and the SM
 // count; the grid of a tile pass is one wave of them (each block loops over
-// tiles), so no block waits for a second wave.  Cached per tile size.
+// tiles), so no block waits for a second wave.  Cached per device and tile
+// size (kernel attributes are per device); callers may be on several threads.
 int tile_launch_shape(int device, int threads, size_t smem, int* resident_out, int* sms_out) {
-  static int sms = 0;
-  static int resident[kTileMaxK + 2] = {};  // by log2 of the tile
-  if (!sms) {
-    SPZ_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device));
+  static std::mutex mu;
+  static int sms[kMaxDevices] = {};
+  static int resident[kMaxDevices][kTileMaxK + 2] = {};  // by log2 of the tile
+  if (device < 0 || device >= kMaxDevices) return fail(SPZ_ERR_INVALID_ARGUMENT, "device index out of range");
+  std::lock_guard<std::mutex> lock(mu);
+  if (!sms[device]) {
+    int count = 0;
+    SPZ_CUDA(cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount, device));
     const int max_smem = (2 << kTileMaxK) * 8 + (1 << (kTileMaxK - kTileLowBits)) * 8;
     SPZ_CUDA(cudaFuncSetAttribute(tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
     SPZ_CUDA(cudaFuncSetAttribute(tile_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
                                   cudaSharedmemCarveoutMaxShared));
+    sms[device] = count;
   }
   int lg = 0;  // the largest lg with 2 x 8 B x 2^lg <= smem (the tile's re and im)
   while (lg <= kTileMaxK && (16ull << (lg + 1)) <= smem) ++lg;
-  int& r = resident[lg];
+  int& r = resident[device][lg];
   if (!r) {
     int per_sm = 0;
     SPZ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tile_kernel, threads, smem));
     r = std::max(1, per_sm);
   }
   *resident_out = r;
-  *sms_out = sms;
+  *sms_out = sms[device];
   return SPZ_OK;
 }
 

@@ -7,6 +7,7 @@
 
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -17,6 +18,8 @@ namespace spz {
 constexpr int kMaxQubits = SPZ_MAX_QUBITS;
 constexpr int kNumSMs = 152;          // GB300: 2 dies x 76 SMs
 constexpr int kThreads = 256;
+// Per-device caches (kernel attributes, launch shapes) hold this many devices.
+constexpr int kMaxDevices = 64;
 
 // ------------------------------------------------------------ error state
 void set_error(const std::string& msg);

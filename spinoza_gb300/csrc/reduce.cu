@@ -521,11 +521,16 @@ static int pauli_tiles(spz_state_t h, const spz_pauli_term* terms, size_t nterms
   double* dpart = dtab + tab.size();
   double* dres = dpart + passes.size() * slots_per_pass;
   SPZ_CUDA(cudaMemcpyAsync(dtab, tab.data(), tab.size() * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-  static bool attr = false;
-  if (!attr) {
-    SPZ_CUDA(cudaFuncSetAttribute(pauli_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  (int)((2 << kPtK) + (1 << (kPtK - kPtLow)) + 64 + (kPtMaxDiag / 8) * (256 + 16)) * 8));
-    attr = true;
+  {  // the shared-memory opt-in, once per device (a per-device kernel attribute)
+    static std::mutex attr_mu;
+    static bool attr[kMaxDevices] = {};
+    if (h->device < 0 || h->device >= kMaxDevices) return fail(SPZ_ERR_INVALID_ARGUMENT, "device index out of range");
+    std::lock_guard<std::mutex> lock(attr_mu);
+    if (!attr[h->device]) {
+      SPZ_CUDA(cudaFuncSetAttribute(pauli_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)((2 << kPtK) + (1 << (kPtK - kPtLow)) + 64 + (kPtMaxDiag / 8) * (256 + 16)) * 8));
+      attr[h->device] = true;
+    }
   }
   for (size_t p = 0; p < passes.size(); ++p) {
     const Pass& P = passes[p];
