@@ -14,6 +14,8 @@ three controls (t+1..t+3) mod n, on every target; 2^15 groups per target, so
 """
 from __future__ import annotations
 
+import gc
+
 import numpy as np
 import pytest
 
@@ -42,6 +44,8 @@ def big_state(gpu):
     import torch
 
     n = N_QUBITS
+    gc.collect()  # states of earlier tests, and torch's cached blocks
+    torch.cuda.empty_cache()
     free, _ = torch.cuda.mem_get_info()
     if free < (16 << n) + (8 << 30):
         pytest.skip(f"needs {16 << n >> 30} GiB of free device memory, {free >> 30} GiB free")
