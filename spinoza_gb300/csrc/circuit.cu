@@ -771,7 +771,74 @@ int run_gates_io(spz_state_t h, const std::vector<GateApp>& gates_in, uint32_t f
     int rc = queue_uploads(passes.empty() ? -1 : pass_slab_q(passes[0]));
     if (rc) return rc;
   }
-  for (size_t p = 0; p < passes.size(); ++p) {
+  // Tiles [part * ntiles / parts, (part + 1) * ntiles / parts) of tile pass p.
+  auto launch_tiles = [&](size_t p, int part, int parts) -> int {
+    const PlannedPass& P = passes[p];
+    PassArgs A{};
+    A.re = h->re;
+    A.im = h->im;
+    A.k = (int)P.local.size();
+    A.c = c;
+    A.nhigh = A.k - c;
+    for (int j = 0; j < A.k; ++j) A.lpos[j] = (uint8_t)P.local[j];
+    const uint64_t ntiles = 1ull << (n - A.k);
+    const uint64_t per = ntiles / parts;
+    A.tile_begin = per * part;
+    A.ntiles = per * (part + 1);
+    A.gates = dgates + offs[p];
+    A.tables = dtables;
+    A.outcomes = h->meas ? reinterpret_cast<const int32_t*>(h->meas + kMeasOutcomeOffset) : nullptr;
+    A.ngates = (int)P.gates.size();
+    const uint32_t T = 1u << A.k;
+    const size_t smem = 2 * T * sizeof(double) + (size_t)(1u << A.nhigh) * sizeof(uint64_t);
+    const int threads = (int)std::min<uint32_t>(kTileThreads, std::max<uint32_t>(32, T / 2));
+    int resident = 0, sms = 0;
+    int rc = tile_launch_shape(h->device, threads, smem, &resident, &sms);
+    if (rc) return rc;
+    const uint64_t blocks = std::min<uint64_t>(per, (uint64_t)sms * resident);
+    tile_kernel<<<(unsigned)blocks, threads, smem, h->stream>>>(A);
+    SPZ_CHECK_LAUNCH("tile_kernel");
+    return SPZ_OK;
+  };
+  // Slab-major prefix: the leading tile passes whose three highest non-local
+  // qubits are the upload's slab qubits all read and write slab j within slab
+  // j's tile range, so they run slab by slab (upload j, passes 0 .. m-1 on slab
+  // j, then slab j + 1), hiding m passes of compute behind the upload instead
+  // of one.  When that covers every pass, each slab's download follows its
+  // last launch.
+  size_t first = 0;
+  if (io && io->in_re && up_q >= 0) {
+    size_t m = 0;
+    while (m < passes.size() && pass_slab_q(passes[m]) == up_q) ++m;
+    if (m >= 2) {
+      const bool all = m == passes.size();
+      const bool down = all && io->out_re;
+      int rc = timer.begin();
+      for (int j = 0; j < kIoChunks && !rc; ++j) {
+        cudaError_t we = cudaStreamWaitEvent(h->stream, io->up[j], 0);
+        if (we != cudaSuccess) rc = cuda_fail(we, "cudaStreamWaitEvent");
+        for (size_t p = 0; p < m && !rc; ++p) rc = launch_tiles(p, j, kIoChunks);
+        if (!rc && down) {
+          cudaError_t re = cudaEventRecord(io->down[j], h->stream);
+          rc = re == cudaSuccess ? io_download(h, io, j, up_q) : cuda_fail(re, "cudaEventRecord");
+        }
+      }
+      uploaded_wait = true;
+      if (!rc) rc = timer.end(true);
+      if (!rc && all && !down) rc = download_all();
+      if (rc) {
+        timer.collect(nullptr);
+        return rc;
+      }
+      if (st) {
+        st->passes += m;
+        st->tile_passes += m;
+        st->bytes_moved += m * (32ull << n);
+      }
+      first = m;
+    }
+  }
+  for (size_t p = first; p < passes.size(); ++p) {
     const PlannedPass& P = passes[p];
     const bool last = p + 1 == passes.size();
     if (!tiled(P)) {
@@ -790,26 +857,6 @@ int run_gates_io(spz_state_t h, const std::vector<GateApp>& gates_in, uint32_t f
       }
       continue;
     }
-    PassArgs A{};
-    A.re = h->re;
-    A.im = h->im;
-    A.k = (int)P.local.size();
-    A.c = c;
-    A.nhigh = A.k - c;
-    for (int j = 0; j < A.k; ++j) A.lpos[j] = (uint8_t)P.local[j];
-    A.ntiles = 1ull << (n - A.k);
-    A.gates = dgates + offs[p];
-    A.tables = dtables;
-    A.outcomes = h->meas ? reinterpret_cast<const int32_t*>(h->meas + kMeasOutcomeOffset) : nullptr;
-    A.ngates = (int)P.gates.size();
-    const uint32_t T = 1u << A.k;
-    const size_t smem = 2 * T * sizeof(double) + (size_t)(1u << A.nhigh) * sizeof(uint64_t);
-    const int threads = (int)std::min<uint32_t>(kTileThreads, std::max<uint32_t>(32, T / 2));
-    int resident = 0, sms = 0;
-    {
-      int rc2 = tile_launch_shape(h->device, threads, smem, &resident, &sms);
-      if (rc2) return rc2;
-    }
     // With host copies to overlap, the first / last pass runs slab by slab
     // (the first pass only in the geometry its uploads were queued in).
     const int sq = pass_slab_q(P);
@@ -823,11 +870,7 @@ int run_gates_io(spz_state_t h, const std::vector<GateApp>& gates_in, uint32_t f
       return rc;
     }
     const int launches = (split_in || split_out) ? kIoChunks : 1;
-    const uint64_t per = A.ntiles / launches;
     for (int j = 0; j < launches; ++j) {
-      PassArgs B = A;
-      B.tile_begin = per * j;
-      B.ntiles = per * (j + 1);
       if (split_in) {
         cudaError_t we = cudaStreamWaitEvent(h->stream, io->up[j], 0);
         if (we != cudaSuccess) {
@@ -835,12 +878,10 @@ int run_gates_io(spz_state_t h, const std::vector<GateApp>& gates_in, uint32_t f
           return cuda_fail(we, "cudaStreamWaitEvent");
         }
       }
-      const uint64_t blocks_j = std::min<uint64_t>(per, (uint64_t)sms * resident);
-      tile_kernel<<<(unsigned)blocks_j, threads, smem, h->stream>>>(B);
-      cudaError_t le = cudaGetLastError();
-      if (le != cudaSuccess) {
+      rc = launch_tiles(p, j, launches);
+      if (rc) {
         timer.collect(nullptr);
-        return cuda_fail(le, "tile_kernel");
+        return rc;
       }
       if (split_out) {
         cudaError_t re = cudaEventRecord(io->down[j], h->stream);

@@ -332,6 +332,42 @@ def test_execute_host_equals_device_execute(gpu, pinned, case):
     assert st.gates == (len(ops) if case != "empty" else 0)
 
 
+def _below_top(n, layers):
+    """Gates on qubits 0 .. n-4 only: every pass keeps the top three qubits
+    non-local, so the whole run goes slab by slab (upload, passes, download)."""
+    qc = _builder()
+    ang = rng.uniforms(17, 3 * n * layers) * 2 * math.pi
+    for layer in range(layers):
+        for q in range(n - 3):
+            qc.u(ang[3 * (layer * n + q)], ang[3 * (layer * n + q) + 1], ang[3 * (layer * n + q) + 2], q)
+        for q in range(n - 4):
+            qc.cx(q, q + 1)
+        qc.cp(0.4, n - 1, 2)  # a control on a slab qubit: a per-tile predicate
+    return qc.ops()
+
+
+@pytest.mark.parametrize("fast", [False, True], ids=["exact", "fast"])
+@pytest.mark.parametrize("case", ["prefix", "all_slabbed"])
+def test_execute_host_slab_major_passes(gpu, case, fast):
+    """Leading passes that keep the upload's slab qubits non-local run slab by
+    slab after each slab's upload (and, when every pass does, each slab's
+    download follows): results equal the device execute bit for bit."""
+    n = 20 if case == "prefix" else 16
+    ops = brickwork(n, 2) if case == "prefix" else _below_top(n, 3)
+    init = rng.normal_state(n, 13)
+    s = State.from_arrays(*init)
+    qc = QuantumCircuit.from_state(s, fast=fast)
+    qc.execute_ops(ops)
+    want = s.to_numpy()
+    for inplace in (True, False):
+        re, im = _host_pair(init, True)
+        out = None if inplace else _host_pair((np.zeros_like(init[0]), np.zeros_like(init[1])), True)
+        st = circuit.execute_host(ops, re, im, out, fast=fast)
+        got = (re, im) if inplace else out
+        assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1])
+        assert st.gates == len(ops) and st.tile_passes >= 2
+
+
 @pytest.mark.parametrize("fast", [False, True], ids=["exact", "fast"])
 def test_execute_host_with_measurements(gpu, fast):
     """Measurements split the run into segments: the upload feeds the first,
