@@ -216,10 +216,11 @@ int spz_circuit_execute(spz_state_t h, const spz_op* ops, size_t nops, spz_track
  * are uploaded into the handle, the circuit runs, and the result is written
  * to the output arrays before the call returns; pass the same arrays for the
  * reference's in-place behaviour.  For page-locked arrays (cudaHostAlloc /
- * cudaHostRegister) the upload is cut into 8 slabs that the first tile pass
- * consumes as they arrive and the download follows the last pass slab by
- * slab, on a second stream; pageable arrays are copied whole before and
- * after.  Same flags, tracker and stats as spz_circuit_execute. */
+ * cudaHostRegister) the upload is cut into 8 slabs that the leading tile
+ * passes consume as they arrive (every leading pass that keeps the slab
+ * qubits non-local runs slab by slab) and the download follows the last pass
+ * slab by slab, on a second stream; pageable arrays are copied whole before
+ * and after.  Same flags, tracker and stats as spz_circuit_execute. */
 int spz_circuit_execute_host(spz_state_t h, const double* in_reals, const double* in_imags, double* out_reals,
                              double* out_imags, const spz_op* ops, size_t nops, spz_tracker* tracker,
                              uint32_t flags, spz_exec_stats* stats);

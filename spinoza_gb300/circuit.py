@@ -321,7 +321,7 @@ def execute_host(ops: np.ndarray, reals: np.ndarray, imags: np.ndarray, out: Opt
     or in place when `out` is None (the reference's behaviour).  Contiguous
     float64 arrays of 2^n; page-locked arrays (e.g.
     ``torch.empty(..., pin_memory=True).numpy()``) get copies that overlap the
-    first and last pass.  `state` supplies the device memory (a new n-qubit
+    leading and last passes.  `state` supplies the device memory (a new n-qubit
     handle when None)."""
     out_re, out_im = out if out is not None else (reals, imags)
     arrs = (reals, imags, out_re, out_im)

@@ -583,8 +583,8 @@ int tile_launch_shape(int device, int threads, size_t smem, int* resident_out, i
 }
 
 // Host arrays that one run of gates uploads from before it and downloads to
-// after it, with the copies overlapping the first and last tile pass where the
-// pass can be cut into kIoChunks slabs: slab j holds the amplitudes whose
+// after it, with the copies overlapping the leading and the last tile passes
+// where a pass can be cut into kIoChunks slabs: slab j holds the amplitudes whose
 // three slab qubits q, q+1, q+2 read j, where those are the pass's three
 // highest non-local qubits; the pass's tiles then fall into slabs by
 // contiguous ranges of tile index.  In memory a slab is 2^(n-q-3) runs of 2^q
@@ -648,7 +648,7 @@ int io_download(spz_state_t h, HostIo* io, int j, int q) {
 }
 
 // Run a list of already validated gate applications on h (with io: host
-// copies before and after, overlapped where the first / last pass allows).
+// copies before and after, overlapped where the leading / last passes allow).
 int run_gates_io(spz_state_t h, const std::vector<GateApp>& gates_in, uint32_t flags, spz_exec_stats* st,
                  HostIo* io) {
   if (gates_in.empty()) return SPZ_OK;
