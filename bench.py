@@ -46,23 +46,43 @@ def measured_peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
-def brickwork_ops(n: int, layers: int, seed: int = 2):
-    from spinoza_gb300 import _native as nat
-    from spinoza_gb300 import rng
+def brickwork_ops(n: int, layers: int, seed: int = 2, source: str = "product"):
+    """The brickwork circuit as a flat op array (the C ABI's spz_op records).
 
-    ang = rng.uniforms(seed, 3 * n * layers) * (2.0 * math.pi)
+    source "product" builds it with the library's own record layout and seeded
+    stream; source "oracle" with the oracle's numpy restatements of both, so
+    that the reference arm never loads the product library.  Both give the
+    same bytes (checked by tests/test_host.py)."""
+    if source == "product":
+        from spinoza_gb300 import _native as mod
+        from spinoza_gb300 import rng
+
+        uniforms = rng.uniforms
+    else:
+        import oracle as mod
+
+        uniforms = mod.uniforms
+    ang = uniforms(seed, 3 * n * layers) * (2.0 * math.pi)
     rows = []
     k = 0
     for _ in range(layers):
         for q in range(n):
-            rows.append(((nat.U, 0, 0, 0, (ang[k], ang[k + 1], ang[k + 2])), q, nat.CONTROLS_NONE, 0, 0))
+            rows.append(((mod.U, 0, 0, 0, (ang[k], ang[k + 1], ang[k + 2])), q, mod.CONTROLS_NONE, 0, 0))
             k += 3
         for q in list(range(0, n - 1, 2)) + list(range(1, n - 1, 2)):
-            rows.append(((nat.X, 0, 0, 0, (0.0, 0.0, 0.0)), q + 1, nat.CONTROLS_SINGLE, 1 << q, 0))
-    ops = np.zeros(len(rows), dtype=nat.OP_DTYPE)
+            rows.append(((mod.X, 0, 0, 0, (0.0, 0.0, 0.0)), q + 1, mod.CONTROLS_SINGLE, 1 << q, 0))
+    ops = np.zeros(len(rows), dtype=mod.OP_DTYPE)
     for i, r in enumerate(rows):
         ops[i] = r
     return ops
+
+
+def workload_config(n: int, layers: int) -> dict:
+    """The `config` object of the headline line, identical in both arms."""
+    return {"workload": f"brickwork-{n}q-{layers}layers (U(theta,phi,lambda) on every qubit, angles U[0,2pi) seed 2, "
+                        f"+ CX even/odd ladders; from |0...0>)",
+            "qubits": n, "layers": layers, "gates": layers * (2 * n - 1), "state_bytes": 16 << n,
+            "l2": "inputs larger than L2 (16 GiB state vs 129 MB L2); no flush"}
 
 
 def replica_throughput(ms_local: float, units_per_replica: float, steps: int, dist=None, device=None):
@@ -82,6 +102,7 @@ def replica_throughput(ms_local: float, units_per_replica: float, steps: int, di
 
 
 def algorithmic_bytes(ops, n: int) -> int:
+    """Unfused algorithmic bytes as the library's planner counts them."""
     from spinoza_gb300 import circuit
 
     return circuit.plan_stats(n, ops, fused=False)["algorithmic_bytes"]
@@ -164,12 +185,13 @@ def profile_traffic(kernel_file: str):
 # ---------------------------------------------------------------- CPU arms
 def cpu_sample(n: int, layers_sample: int, reps: int = 1, warmup: int = 0) -> dict:
     """The oracle (restated reference CPU path, OpenMP over all host cores) on
-    `layers_sample` brickwork layers at n qubits; returns GB/s over the
-    sample's algorithmic bytes."""
+    `layers_sample` brickwork layers at n qubits; returns the sample's
+    algorithmic bytes and times.  Touches only the oracle: the ops, the seeded
+    angles and the byte count all come from its numpy restatements."""
     import oracle
 
-    ops = brickwork_ops(n, layers_sample)
-    abytes = algorithmic_bytes(ops, n)
+    ops = brickwork_ops(n, layers_sample, source="oracle")
+    abytes = oracle.algorithmic_bytes(ops, n)
     re, im = oracle.zero_state(n)
     times = []
     for r in range(warmup + reps):
@@ -193,14 +215,17 @@ def reference_arm(args) -> None:
     res = cpu_sample(n, 1, reps=args.steps, warmup=args.warmup)
     t = sum(res["times"])
     value = res["bytes"] * len(res["times"]) / t / 1e9
+    ms_layer = 1e3 * t / len(res["times"])
     sample = (f"1 of {layers} brickwork layers per step ({res['gates']} of {layers * (2 * n - 1)} gates) at {n} "
-              f"qubits, oracle restatement of the reference CPU path (reference Rust crate not buildable here)")
+              f"qubits: the layers have identical structure, so GB/s over one layer is the full circuit's rate and "
+              f"a full step takes {layers} x the layer time; oracle restatement of the reference CPU path "
+              f"(reference Rust crate not buildable here), OpenMP over {res['threads']} host threads")
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / len(res["times"]),
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_layer,
+        "ms_per_full_circuit_extrapolated": ms_layer * layers,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"brickwork-{n}q-{layers}layers (U on every qubit + CX even/odd, from |0...0>)",
-                   "qubits": n, "layers": layers, "sample_layers_per_step": 1},
+        "config": workload_config(n, layers),
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": res["threads"], "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -403,14 +428,11 @@ def gpu_arm(args) -> None:
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"brickwork-{n}q-{layers}layers (U(theta,phi,lambda) on every qubit, angles "
-                                   f"U[0,2pi) seed 2, + CX even/odd ladders; from |0...0>)",
-                       "qubits": n, "layers": layers, "gates": int(len(ops)), "state_bytes": 16 * N,
-                       "l2": "inputs larger than L2 (16 GiB state vs 129 MB L2); no flush",
-                       "executor": ("fused shared-memory tile passes, exact reference arithmetic" if args.exact else
-                                    "fused shared-memory tile passes, fast arithmetic (lazy scaling, U = P RY P, "
-                                    "phases pushed through permutations); equal to exact up to rounding"),
-                       "parallelism": "replicas" if world > 1 else "single-gpu"},
+            "config": workload_config(n, layers),
+            "executor": ("fused shared-memory tile passes, exact reference arithmetic" if args.exact else
+                         "fused shared-memory tile passes, fast arithmetic (lazy scaling, U = P RY P, phases pushed "
+                         "through permutations); equal to exact up to rounding"),
+            "parallelism": "replicas" if world > 1 else "single-gpu",
             "gates_per_s": len(ops) * world * args.steps / (ms / 1e3),
             "passes_per_step": int(launches / args.steps) - 1,
             "roofline": {"bound": "hbm", "kernel": "tile_kernel", "achieved": achieved, "peak": peaks["hbm_gbs"],

@@ -275,15 +275,19 @@ int spz_xyz_expectation_value(spz_state_t h, char observable, const uint32_t* ta
 
 /* Allocation-free form of spz_xyz_expectation_value.  It has no counterpart in
  * the reference.  It is for callers that cannot call cudaMalloc: code that runs
- * inside another framework's memory pool or arena, inside a CUDA-graph capture
- * that must not allocate, or in a process with a fixed memory budget.  It takes
- * the state as raw device arrays (2^n doubles each) instead of a handle, runs on
- * `stream` (a cudaStream_t, NULL = default stream) and writes ntargets results
- * to `out` (host or device memory); it synchronises `stream` before returning.
- * Its scratch is a static 10 KiB device array that every GPU loading the library
- * holds until exit, so at most SPZ_NOALLOC_MAX_TARGETS targets per call; more
- * returns SPZ_ERR_INVALID_ARGUMENT.  The first call on a device looks up the
- * array's address on that device: make it before any stream capture.  All calls
+ * inside another framework's memory pool or arena (where a stray cudaMalloc
+ * would bypass the pool's accounting or fail against its reservation), or in a
+ * process whose device memory budget is fixed up front.  It takes the state as
+ * raw device arrays (2^n doubles each) instead of a handle, runs on `stream`
+ * (a cudaStream_t, NULL = default stream), writes ntargets results to `out`
+ * (host or device memory), and synchronises `stream` before returning.
+ * Its scratch is a static 10 KiB device array that every GPU loading the
+ * library holds until exit, so at most SPZ_NOALLOC_MAX_TARGETS targets per
+ * call; more returns SPZ_ERR_INVALID_ARGUMENT.  ntargets == 0 returns SPZ_OK
+ * and launches nothing.  The first call on a device looks up the array's
+ * address on that device and keeps it for the life of the process; make that
+ * first call before any stream capture, and do not call this function on a
+ * device after cudaDeviceReset (the kept address would be stale).  All calls
  * share the array: calls that overlap on the GPU race and must be serialised. */
 #define SPZ_NOALLOC_MAX_TARGETS 64
 int spz_xyz_expectation_value_noalloc(const double* d_reals, const double* d_imags, uint32_t n,

@@ -192,4 +192,51 @@ def num_threads() -> int:
     return lib().orc_num_threads()
 
 
+# --------------------------------------------------------------------------
+# numpy restatements used where the product library must not be loaded (the
+# benchmark's reference arm): the op record layout, the seeded uniform stream
+# and the per-gate algorithmic byte counts.
+
+GATE_DTYPE = np.dtype([("kind", "<i4"), ("q0", "<u4"), ("q1", "<u4"), ("pad_", "<u4"), ("p", "<f8", (3,))])
+# Same 64-byte record as `struct Op` in spz_oracle.cpp (the flat form of the
+# reference's QuantumTransformation, circuit.rs:113-120).
+OP_DTYPE = np.dtype([("gate", GATE_DTYPE), ("target", "<u4"), ("controls_kind", "<i4"),
+                     ("controls", "<u8"), ("zeros", "<u8")])
+CONTROLS_NONE, CONTROLS_SINGLE, CONTROLS_ONES, CONTROLS_MIXED = range(4)
+
+_GOLDEN = np.uint64(0x9E3779B97F4A7C15)
+
+
+def _mix64(z: np.ndarray) -> np.ndarray:
+    z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+    z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+    return z ^ (z >> np.uint64(31))
+
+
+def uniforms(seed: int, count: int, start: int = 0) -> np.ndarray:
+    """Uniforms [start, start + count) of the seeded splitmix64 stream, the same
+    values as orc_stream_uniform (53 random bits each)."""
+    with np.errstate(over="ignore"):
+        key = _mix64(np.array([seed], dtype=np.uint64) + _GOLDEN)[0]
+        idx = np.arange(start + 1, start + count + 1, dtype=np.uint64)
+        return (_mix64(key + idx * _GOLDEN) >> np.uint64(11)).astype(np.float64) * (2.0 ** -53)
+
+
+def algorithmic_bytes(ops: np.ndarray, n: int) -> int:
+    """Sum over the ops of the bytes one unfused pass of that gate must read and
+    write on 2^n FP64 SoA amplitudes: every amplitude (32 N) for a gate that
+    mixes or rephases both halves, half of them (16 N) for Z, P and SWAP, and
+    2^-k of that under k controls.  Measurements are not counted."""
+    N = 1 << n
+    total = 0
+    for op in ops:
+        kind = int(op["gate"]["kind"])
+        nc = bin(int(op["controls"])).count("1") if int(op["controls_kind"]) != CONTROLS_NONE else 0
+        if kind == M:
+            continue
+        full = 16 * N if kind in (Z, P, SWAP) else 32 * N
+        total += full >> nc
+    return total
+
+
 _ = Path

@@ -1,17 +1,21 @@
 // spz_xyz_expectation_value_noalloc: <X>, <Y> or <Z> per target without any
 // device allocation, for callers that cannot call cudaMalloc — code running
-// inside another framework's memory pool or arena, inside a CUDA-graph capture
-// that must not allocate, or in a process whose memory budget is fixed up front.
+// inside another framework's memory pool or arena, whose accounting a stray
+// cudaMalloc would bypass, or in a process whose memory budget is fixed up
+// front.
 //
 // The reduction's scratch (block partials and one result slot per target)
 // lives in the file-scope array below, 10 KiB per GPU that loads the library,
 // held until the process exits.  Its device address is looked up once per
 // device (cudaGetSymbolAddress, with that device current) on the first call
-// made on that device; make that first call before any stream capture.
-// Every call shares the one array, so calls that overlap on the GPU (on
-// different streams or host threads) race with each other and must be
-// serialised by the caller.  The block partials are fully rewritten by each
-// call and each slot is written before it is read, so nothing needs clearing.
+// made on that device, and kept for the life of the process: make that first
+// call before any stream capture, and make no call on a device after
+// cudaDeviceReset, which would leave the kept address stale.  Every call
+// shares the one array, so calls that overlap on the GPU (on different
+// streams or host threads) race with each other and must be serialised by the
+// caller.  The block partials are fully rewritten by each call and each slot
+// is written before it is read, so nothing needs clearing.  The call ends by
+// copying the results to `out` and synchronising the stream.
 #include <algorithm>
 #include <mutex>
 

@@ -7,7 +7,7 @@ numeric array literal (`let vals = [...]`, `let expected_reals = [...]`) with
 its file:line.  tests/test_oracle_golden.py restates each test's setup and
 checks the oracle (and the GPU path) against these values.
 
-Usage:  python tests/golden/extract_reference_goldens.py [/path/to/reference]
+Usage:  python tests/golden/extract_reference_goldens.py <path of a checkout of the reference>
 """
 from __future__ import annotations
 
@@ -80,7 +80,9 @@ def parse_file(root: Path, rel: str) -> dict:
 
 
 def main() -> None:
-    root = Path(sys.argv[1]) if len(sys.argv) > 1 else Path("/root/reference")
+    if len(sys.argv) < 2:
+        sys.exit("usage: extract_reference_goldens.py <path of a checkout of the reference repository>")
+    root = Path(sys.argv[1])
     goldens = {"source": "QuState/spinoza v0.5.1 (spinoza/Cargo.toml:3), Rust #[test] modules",
                "extracted_by": "tests/golden/extract_reference_goldens.py", "tests": {}}
     for rel in FILES:

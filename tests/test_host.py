@@ -226,3 +226,44 @@ def test_circuit_builders_mirror_reference(native):
     qc.p(math.pi / 4, 1)
     qc.inverse()
     assert qc.transformations[0].gate == Gate.P(-math.pi / 4) and qc.transformations[1].gate == Gate.H
+
+
+# ------------------------------------------------------- benchmark reference arm
+def test_bench_arms_build_the_same_workload(native):
+    """The reference arm builds its ops and byte count from the oracle's numpy
+    restatements; they must equal the product-side ones bit for bit."""
+    import bench
+
+    a = bench.brickwork_ops(12, 3, source="product")
+    b = bench.brickwork_ops(12, 3, source="oracle")
+    assert a.dtype.itemsize == b.dtype.itemsize == 64
+    assert a.tobytes() == b.tobytes()
+    assert oracle.algorithmic_bytes(b, 12) == bench.algorithmic_bytes(a, 12)
+    assert bench.workload_config(30, 20)["gates"] == len(bench.brickwork_ops(30, 20, source="oracle"))
+
+
+def test_oracle_uniforms_match_the_c_stream():
+    u = oracle.uniforms(99, 16, start=5)
+    assert all(u[i] == oracle.stream_uniform(99, 5 + i) for i in range(16))
+
+
+def test_reference_arm_does_not_load_the_product_library():
+    """`bench.py --impl reference` must run the oracle only: neither the
+    spinoza_gb300 package nor its shared library may be loaded."""
+    import json
+    import subprocess
+    import sys
+
+    root = Path(__file__).resolve().parent.parent
+    code = ("import sys, json; sys.argv = ['bench.py', '--impl', 'reference', '--qubits', '12', '--layers', '4', "
+            "'--steps', '2', '--warmup', '1']; import bench; bench.main(); "
+            "maps = open('/proc/self/maps').read(); "
+            "print(json.dumps({'pkg': [m for m in sys.modules if m.startswith('spinoza_gb300')], "
+            "'so': 'libspinoza_gb300' in maps}))")
+    out = subprocess.run([sys.executable, "-c", code], cwd=root, capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr
+    lines = [json.loads(x) for x in out.stdout.splitlines() if x.startswith("{")]
+    line, probe = lines[0], lines[-1]
+    assert line["impl"] == "reference" and line["value"] > 0
+    assert line["config"] == __import__("bench").workload_config(12, 4)
+    assert probe == {"pkg": [], "so": False}
