@@ -183,7 +183,7 @@ def profile_traffic(kernel_file: str):
 
 
 # ---------------------------------------------------------------- CPU arms
-def cpu_sample(n: int, layers_sample: int, reps: int = 1, warmup: int = 0) -> dict:
+def cpu_sample(n: int, layers_sample: int, reps: int = 1, warmup: int = 0, keep_state: bool = False) -> dict:
     """The oracle (restated reference CPU path, OpenMP over all host cores) on
     `layers_sample` brickwork layers at n qubits; returns the sample's
     algorithmic bytes and times.  Touches only the oracle: the ops, the seeded
@@ -203,8 +203,10 @@ def cpu_sample(n: int, layers_sample: int, reps: int = 1, warmup: int = 0) -> di
         dt = time.perf_counter() - t0
         if r >= warmup:
             times.append(dt)
-    del re, im
-    return {"bytes": abytes, "times": times, "gates": len(ops), "threads": oracle.num_threads()}
+    out = {"bytes": abytes, "times": times, "gates": len(ops), "threads": oracle.num_threads()}
+    if keep_state:
+        out["state"] = (re, im)
+    return out
 
 
 def reference_arm(args) -> None:
@@ -285,6 +287,86 @@ def adjoint_bench(n: int = 24, layers: int = 8, fd_sample: int = 4) -> dict:
             "speedup_vs_fd": t_fd / t_adj, "fd_sample": f"{fd_sample} of {2 * len(pidx)} forward circuits"}
 
 
+def sweep_single_qubit(state, n: int, peak_gbs: float, fma_rate: float, reps: int = 3) -> dict:
+    """Every single-qubit gate kind on every target at n qubits, through
+    spz_apply: the reference's arithmetic (default) and the opt-in lazy mode
+    (H, RX, RY as the gate over a scalar; RZ as P on the 1 half times a
+    carried phase).  Per gate: CUDA-event time on the state's stream (mean of
+    `reps` back-to-back applications), GB/s over the algorithmic 32 N bytes,
+    the fraction of the measured HBM copy rate and of the live DFMA rate."""
+    import torch
+
+    from spinoza_gb300 import gates
+    from spinoza_gb300.gates import Gate
+
+    N = 1 << n
+    kinds = [("H", Gate.H, 8, 4), ("RX", Gate.RX(0.7), 12, 4), ("RY", Gate.RY(0.7), 12, 4),
+             ("RZ", Gate.RZ(0.7), 8, 4), ("U", Gate.U(0.3, 0.4, 0.5), 14, None), ("X", Gate.X, 0, None)]
+    stream = torch.cuda.current_stream()
+    rows = []
+    for lazy in (False, True):
+        state.set_lazy(lazy)
+        for name, g, fp_exact, fp_lazy in kinds:
+            if lazy and fp_lazy is None:
+                continue
+            for t in range(n):
+                gates.apply(g, state, t)  # warm-up
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                for _ in range(reps):
+                    gates.apply(g, state, t)
+                e1.record(stream)
+                e1.synchronize()
+                ms = e0.elapsed_time(e1) / reps
+                fp = (fp_lazy if lazy else fp_exact) * (N // 2)
+                gbs = 32 * N / (ms / 1e3) / 1e9
+                rows.append({"gate": name, "mode": "lazy" if lazy else "exact", "target": t, "ms": ms, "gbs": gbs,
+                             "hbm_frac": gbs / peak_gbs, "fp64_frac": fp / (ms / 1e3) / fma_rate})
+            state.settle()
+    state.set_lazy(False)
+    summary = {}
+    for name, _, _, _ in kinds:
+        for mode in ("exact", "lazy"):
+            r = [x for x in rows if x["gate"] == name and x["mode"] == mode]
+            if not r:
+                continue
+            summary[f"{name}_{mode}"] = {
+                "ms_median": statistics.median(x["ms"] for x in r),
+                "gbs_median": statistics.median(x["gbs"] for x in r),
+                "hbm_frac_median": statistics.median(x["hbm_frac"] for x in r),
+                "hbm_frac_min": min(x["hbm_frac"] for x in r),
+                "fp64_frac_median": statistics.median(x["fp64_frac"] for x in r)}
+    return {"qubits": n, "reps": reps, "peak_gbs": peak_gbs, "fma_rate": fma_rate, "summary": summary,
+            "rows": rows,
+            "note": "GB/s = 32 N algorithmic bytes per gate / time (the lazy RZ moves only the 1 half, 16 N); "
+                    "exact = the reference's arithmetic, bit-identical; lazy = spz_state_set_lazy, within rounding"}
+
+
+def numa_bind_to_gpu(device: int) -> dict:
+    """Run this thread on the host cores of the GPU's NUMA node, so that pinned
+    host buffers allocated afterwards are first touched (placed) there."""
+    info = {"nproc": os.cpu_count(), "node": None, "cpus": None}
+    try:
+        import torch
+
+        pr = torch.cuda.get_device_properties(device)
+        bus = f"{int(getattr(pr, 'pci_domain_id', 0)):04x}:{int(pr.pci_bus_id):02x}:{int(pr.pci_device_id):02x}.0"
+        info["pci"] = bus
+        node = int(Path(f"/sys/bus/pci/devices/{bus}/numa_node").read_text().strip())
+        info["node"] = node
+        if node >= 0:
+            cpus = set()
+            for part in Path(f"/sys/devices/system/node/node{node}/cpulist").read_text().strip().split(","):
+                lo, _, hi = part.partition("-")
+                cpus.update(range(int(lo), int(hi or lo) + 1))
+            if cpus:
+                os.sched_setaffinity(0, cpus)
+                info["cpus"] = len(cpus)
+    except (OSError, ValueError, AttributeError, RuntimeError) as e:
+        info["error"] = str(e)
+    return info
+
+
 def gpu_arm(args) -> None:
     import torch
 
@@ -356,6 +438,7 @@ def gpu_arm(args) -> None:
     # end to end: host (pinned) |0...0> in, execute, host result out
     e2e = None
     if not args.no_e2e:
+        numa = numa_bind_to_gpu(local)
         hin_re = torch.zeros(N, dtype=torch.float64, pin_memory=True)
         hin_im = torch.zeros(N, dtype=torch.float64, pin_memory=True)
         hin_re[0] = 1.0
@@ -386,6 +469,7 @@ def gpu_arm(args) -> None:
         e2e = {"value": abytes * world / t_e2e / 1e9, "unit": UNIT, "h2d_bytes_per_step": 16 * N + ops.nbytes,
                "d2h_bytes_per_step": 16 * N, "ms_per_step": 1e3 * t_e2e,
                "upload_alone_ms": 1e3 * (t2 - t1), "download_alone_ms": 1e3 * (t3 - t2),
+               "h2d_gbs": 16 * N / (t2 - t1) / 1e9, "d2h_gbs": 16 * N / (t3 - t2) / 1e9, "host": numa,
                "api": "spz_circuit_execute_host (pinned host arrays in and out; the copies overlap the first "
                       "and last tile pass, slab by slab)"}
         del hin_re, hin_im, hout_re, hout_im
@@ -414,15 +498,40 @@ def gpu_arm(args) -> None:
                   "exact_gbs": abytes / (t0.elapsed_time(t1) / 1e3) / 1e9,
                   "max_abs_amplitude": max(float(re_t.abs().max()), float(im_t.abs().max()))}
         del s2, q2, re2, im2
+    sweep = None
+    if rank == 0 and not args.no_sweep:
+        sweep = sweep_single_qubit(state, n, peaks["hbm_gbs"], fma_rate)
     adj = None if args.no_adjoint or rank != 0 else adjoint_bench()
+    bat = None if args.no_batch or rank != 0 else batch_bench(args)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        del state, qc
         torch.cuda.synchronize()
-        res = cpu_sample(n, 1)
+        res = cpu_sample(n, 1, keep_state=True)
         cpu = {"value": res["bytes"] / res["times"][0] / 1e9, "unit": UNIT, "cores": res["threads"], "kind": "port",
                "sample": f"1 of {layers} brickwork layers ({res['gates']} gates) at {n} qubits, oracle restatement of "
                          f"the reference CPU path, OpenMP over {res['threads']} host threads"}
+        # Parity of the timed workload against the oracle at full size, on the
+        # same one-layer prefix (outside the timed region): the oracle's state
+        # is uploaded and compared on the device.
+        ore = torch.from_numpy(res["state"][0]).to("cuda")
+        oim = torch.from_numpy(res["state"][1]).to("cuda")
+        del res
+        ops1 = brickwork_ops(n, 1)
+        out = {"prefix": f"first 1 of {layers} layers ({len(ops1)} gates), {n} qubits, from |0...0>"}
+        for mode, fast in (("fast", True), ("exact", False)):
+            state.reset_zero()
+            QuantumCircuit.from_state(state, fast=fast).execute_ops(ops1)
+            torch.cuda.synchronize()
+            d = max(float((re_t - ore).abs().max()), float((im_t - oim).abs().max()))
+            out[f"max_abs_diff_{mode}_vs_oracle"] = d
+            if not fast:
+                out["exact_bit_identical"] = bool(torch.equal(re_t, ore) and torch.equal(im_t, oim))
+        out["bound"] = 1e-12
+        out["ok"] = out["max_abs_diff_fast_vs_oracle"] <= 1e-12 and out["exact_bit_identical"]
+        del ore, oim
+        if parity is None:
+            parity = {}
+        parity["vs_oracle"] = out
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -446,11 +555,13 @@ def gpu_arm(args) -> None:
                              "rate measured live on this GPU before and after the timed region "
                              "(spz_probe_fp64_fma_rate), the larger of the two"},
             "parity": parity,
+            "sweep30": sweep,
             "cpu_baseline": cpu,
             "e2e": e2e,
             "gpu_launches": int(launches),
             "clocks": clk.summary(),
             "adjoint": adj,
+            "batch": bat,
         }
         print(json.dumps(line), flush=True)
     if dist:
@@ -568,8 +679,13 @@ def workload_measure28(args) -> None:
           expectation_gbs=(16 * N) / t_h / 1e9, energy=core.pauli_expectation(s, H))
 
 
-def workload_batch(args) -> None:
-    """Config 5: 4096 instances, qubits 10..22, depth 2..10; one persistent launch vs a loop."""
+def batch_bench(args) -> dict:
+    """Config 5: 4096 instances, qubits 10..22, depth 2..10, forward <H> and
+    adjoint gradients of all of them per graph launch, against a loop of the
+    single-instance path (spz_adjoint_gradient, one instance at a time) on a
+    stratified sample, and against the oracle's parameter shift on sampled
+    instances and parameters."""
+    import oracle
     from spinoza_gb300 import adjoint, batch
     from spinoza_gb300.core import State
 
@@ -577,15 +693,18 @@ def workload_batch(args) -> None:
     insts = batch.config5_instances(args.instances, qmax=args.batch_qmax)
     t_build = time.perf_counter() - t0
     tune = (batch.autotune(insts, reps=1) if args.autotune
-            else {"tile_qubits": args.batch_tile, "threads": args.batch_threads})
-    b = batch.Batch(insts, tile_qubits=tune["tile_qubits"], threads=tune["threads"], wide_qubits=args.batch_wide,
-                    fast=args.batch_fast)
-    b.run()
+            else {"tile_qubits": args.batch_tile, "threads": args.batch_threads, "tiles_per_item": args.batch_tpi})
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    b = batch.Batch(insts, tile_qubits=tune["tile_qubits"], threads=tune["threads"], wide_qubits=args.batch_wide,
+                    fast=args.batch_fast, tiles_per_item=tune.get("tiles_per_item", 0))
+    t_plan = time.perf_counter() - t0
+    b.run()
+    steps = max(1, args.batch_steps)
+    t0 = time.perf_counter()
+    for _ in range(steps):
         e, g = b.run()
-    t_batch = (time.perf_counter() - t0) / args.steps
-    # baseline: the per-instance path (spz_adjoint_gradient) on a stratified sample
+    t_batch = (time.perf_counter() - t0) / steps
+    # the loop: the single-instance path on a stratified sample, extrapolated
     order = sorted(range(len(insts)), key=lambda i: insts[i][0] * 1000 + len(insts[i][1]))
     sample = order[:: max(1, len(order) // args.loop_sample)]
     t_loop_sample = 0.0
@@ -599,15 +718,46 @@ def workload_batch(args) -> None:
         max_e = max(max_e, abs(e1 - e[i]))
         max_g = max(max_g, float(np.max(np.abs(g1 - b.split(g)[i]))))
     t_loop = t_loop_sample * len(insts) / len(sample)
+    # the oracle's parameter shift (exact for RY / RZ) on sampled instances
+    checks, max_ps = 0, 0.0
+    picks = [order[0], order[len(order) // 3], order[-1]]
+    for i in picks:
+        n, ops, pidx, theta, terms = insts[i]
+        gi = b.split(g)[i]
+
+        def energy(th):
+            re, im = oracle.zero_state(n)
+            oracle.execute(adjoint.set_params(ops, pidx, th).view(oracle.OP_DTYPE), re, im)
+            return oracle.pauli_expectation(re, im, terms)
+
+        for j in (0, len(pidx) // 2, len(pidx) - 1):
+            tp, tm = theta.copy(), theta.copy()
+            tp[j] += math.pi / 2
+            tm[j] -= math.pi / 2
+            max_ps = max(max_ps, abs(gi[j] - 0.5 * (energy(tp) - energy(tm))))
+            checks += 1
     nparams = int(b.theta.size)
-    _line("config5 batched forward+adjoint instances/s", len(insts) / t_batch, "instances/s", args,
-          higher_is_better=True,
-          config={"workload": f"{len(insts)} HEA instances (RY/RZ layers + CZ ring), qubits U{{10..{args.batch_qmax}}}, depth "
-                              f"U{{2..10}}, seeds 8+k", "params": nparams, "launch": tune,
-                  "wide_qubits": args.batch_wide or 18, "wide_adjoint": "fast" if args.batch_fast else "exact"},
-          seconds_per_batch=t_batch, grads_per_s=nparams / t_batch, loop_seconds_extrapolated=t_loop,
-          loop_sample=len(sample), speedup_vs_loop=t_loop / t_batch, max_abs_energy_diff=max_e,
-          max_abs_grad_diff=max_g, build_seconds=t_build, info=b.info())
+    qs = [x[0] for x in insts]
+    return {"workload": f"{len(insts)} HEA instances (RY/RZ layers + CZ ring), qubits U{{10..{args.batch_qmax}}}, "
+                        f"depth U{{2..10}}, seeds 8+k", "instances": len(insts), "params": nparams,
+            "qubits_min": min(qs), "qubits_max": max(qs), "launch": tune,
+            "wide_qubits": args.batch_wide or 18, "wide_adjoint": "fast" if args.batch_fast else "exact",
+            "seconds_per_batch": t_batch, "instances_per_s": len(insts) / t_batch, "grads_per_s": nparams / t_batch,
+            "loop_seconds_extrapolated": t_loop, "loop_sample": len(sample), "speedup_vs_loop": t_loop / t_batch,
+            "max_abs_energy_diff_vs_loop": max_e, "max_abs_grad_diff_vs_loop": max_g,
+            "max_abs_grad_diff_vs_oracle_parameter_shift": max_ps, "oracle_checks": checks,
+            "oracle_instances": [int(insts[i][0]) for i in picks],
+            "build_seconds": t_build, "plan_seconds": t_plan, "info": b.info(),
+            "note": "loop = spz_adjoint_gradient per instance (fused executor, one instance at a time), timed on a "
+                    "stratified sample and extrapolated; the batch is one graph launch (coefficients, the persistent "
+                    "kernel with every instance, the fold of the wide instances' partial sums)"}
+
+
+def workload_batch(args) -> None:
+    d = batch_bench(args)
+    _line("config5 batched forward+adjoint instances/s", d["instances_per_s"], "instances/s", args,
+          higher_is_better=True, config={"workload": d["workload"], "params": d["params"], "launch": d["launch"]},
+          batch=d)
 
 
 def workload_sweep33(args) -> None:
@@ -660,6 +810,9 @@ def main() -> None:
     ap.add_argument("--instances", type=int, default=4096)
     ap.add_argument("--loop-sample", type=int, default=64)
     ap.add_argument("--autotune", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="headline line without the config-5 batch object")
+    ap.add_argument("--batch-steps", type=int, default=1, help="timed runs of the config-5 batch")
+    ap.add_argument("--batch-tpi", type=int, default=0, help="batch workload: tiles per work item of a wide instance")
     ap.add_argument("--batch-tile", type=int, default=11, help="batch workload: tile qubits (resident up to this n)")
     ap.add_argument("--batch-threads", type=int, default=128, help="batch workload: threads per block")
     ap.add_argument("--batch-qmax", type=int, default=22, help="batch workload: largest instance (small profiling cases)")
@@ -671,6 +824,7 @@ def main() -> None:
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-parity", action="store_true")
+    ap.add_argument("--no-sweep", action="store_true", help="skip the per-gate sweep at the headline's qubit count")
     ap.add_argument("--exact", action="store_true", help="time the bit-exact executor mode instead of fast mode")
     args = ap.parse_args()
     if args.impl == "reference":

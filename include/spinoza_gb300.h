@@ -123,6 +123,28 @@ int spz_state_copy(spz_state_t dst, spz_state_t src);
  * `normalise` is non-zero the state is scaled to unit norm. */
 int spz_state_fill_random(spz_state_t h, uint64_t seed, int dist, int normalise);
 
+/* Lazy per-gate mode (opt-in; no reference counterpart).  With enable != 0,
+ * spz_apply applies uncontrolled H, RX and RY as the gate divided by a real
+ * scalar (1/sqrt 2, or the larger in magnitude of cos and sin of theta/2): 4
+ * FP64 instructions per amplitude pair instead of the reference's 8-12
+ * (h_apply_strat2 gates.rs:547-562, rx_apply_target :713-725,
+ * ry_apply_strategy2 :1116-1119), which makes them bound by HBM instead of by
+ * FP64 issue on GB300; uncontrolled RZ becomes P (the 1 half only) times a
+ * phase.  The handle carries the product of those scalars and phases as a
+ * pending factor and folds it into the arrays (one scaling pass) before
+ * anything reads them: download, device_arrays, copy, measurement,
+ * expectations, sampling, circuit execution, adjoint differentiation.  Every
+ * other gate runs exactly as in the default mode (a linear gate commutes with
+ * the factor).  Results equal the default mode's up to rounding, not bit for
+ * bit.  Code that reads wrapped arrays (spz_state_wrap) itself must call
+ * spz_state_settle first.  enable == 0 settles and returns to the reference's
+ * arithmetic, the default. */
+int spz_state_set_lazy(spz_state_t h, int enable);
+
+/* Fold the lazy mode's pending factor into the arrays now (nothing to do when
+ * there is none). */
+int spz_state_settle(spz_state_t h);
+
 /* --------------------------------------------------------- gate application */
 /* apply(gate, &mut State, target): uncontrolled gate.
  * Replaces spinoza/src/gates.rs:215-232.  SWAP takes its qubits from the gate
@@ -336,9 +358,12 @@ int spz_adjoint_gradient(spz_state_t h, const spz_op* ops, size_t nops,
 /* Many independent parameterised circuits of uneven qubit counts, each with its
  * own Pauli-sum observable: E_i = <0|U_i(theta)^dagger H_i U_i(theta)|0> and
  * dE_i/dtheta for all of them in one persistent launch, replayed as a CUDA
- * graph.  Instances of up to tile_qubits qubits run entirely in shared memory;
- * larger ones stream tiles through per-CTA workspace.  No reference
- * counterpart (new form). */
+ * graph.  Instances of up to tile_qubits qubits run entirely in shared memory,
+ * one CTA each; larger ones stream tiles through HBM workspace.  Wide
+ * instances (at least wide_qubits qubits) are spread over many CTAs as work
+ * items (one pass over a range of tiles each), ordered by per-instance
+ * completion counters inside the same launch; a dependency wait that runs out
+ * ends the launch with SPZ_ERR_TIMEOUT.  No reference counterpart (new form). */
 typedef struct spz_batch_s* spz_batch_t;
 
 typedef struct spz_batch_instance {
@@ -354,18 +379,27 @@ typedef struct spz_batch_instance {
 typedef struct spz_batch_config {
   int32_t tile_qubits;    /* local qubits per shared-memory tile, 4..12 (0 = 11) */
   int32_t threads;        /* threads per CTA, multiple of 32 in 64..1024 (0 = 128) */
-  int32_t wide_qubits;    /* instances of at least this many qubits run one at a time
-                             across the whole GPU (fused passes + fused adjoint sweep)
-                             instead of one per CTA; 0 = 18, > 30 = never            */
+  int32_t wide_qubits;    /* instances of at least this many qubits (and more than
+                             tile_qubits) are split into work items across CTAs, each
+                             with its own psi and lam in HBM; 0 = 18, > 30 = never.
+                             Those whose workspace exceeds 60% of free memory, and all
+                             of them under SPZ_EXEC_FAST, run one at a time across
+                             the GPU instead (fused executor + fused adjoint sweep) */
   int32_t flags;          /* SPZ_EXEC_FAST: the wide instances use the fast adjoint
                              (equal to the exact one up to rounding)                 */
+  int32_t tiles_per_item; /* tiles per work item of a wide instance (0 = 16)       */
 } spz_batch_config;
 
 typedef struct spz_batch_stats {
-  uint64_t instances, resident_instances;  /* (wide instances count in neither pass total) */
+  uint64_t instances, resident_instances;
   uint64_t forward_passes, hamiltonian_passes, backward_passes;
   uint64_t ctas, workspace_bytes;
   int32_t tile_qubits, threads;
+  uint64_t wide_in_kernel;        /* wide instances run as work items in the launch   */
+  uint64_t work_items;            /* entries of the persistent kernel's queue         */
+  uint64_t wide_separate;         /* wide instances run one at a time across the GPU  */
+  uint64_t wide_workspace_bytes;  /* HBM of the in-launch wide instances' psi and lam */
+  int32_t tiles_per_item, pad_;
 } spz_batch_stats;
 
 /* Plan and upload a batch.  param_index[param_offset + j] is the op (relative to

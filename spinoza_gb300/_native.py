@@ -84,13 +84,16 @@ class spz_batch_instance(ctypes.Structure):
 
 
 class spz_batch_config(ctypes.Structure):
-    _fields_ = [("tile_qubits", c_int32), ("threads", c_int32), ("wide_qubits", c_int32), ("flags", c_int32)]
+    _fields_ = [("tile_qubits", c_int32), ("threads", c_int32), ("wide_qubits", c_int32), ("flags", c_int32),
+                ("tiles_per_item", c_int32)]
 
 
 class spz_batch_stats(ctypes.Structure):
     _fields_ = [("instances", c_uint64), ("resident_instances", c_uint64), ("forward_passes", c_uint64),
                 ("hamiltonian_passes", c_uint64), ("backward_passes", c_uint64), ("ctas", c_uint64),
-                ("workspace_bytes", c_uint64), ("tile_qubits", c_int32), ("threads", c_int32)]
+                ("workspace_bytes", c_uint64), ("tile_qubits", c_int32), ("threads", c_int32),
+                ("wide_in_kernel", c_uint64), ("work_items", c_uint64), ("wide_separate", c_uint64),
+                ("wide_workspace_bytes", c_uint64), ("tiles_per_item", c_int32), ("pad_", c_int32)]
 
 
 INSTANCE_DTYPE = np.dtype([("n", "<u4"), ("nops", "<u4"), ("nparams", "<u4"), ("nterms", "<u4"),
@@ -123,6 +126,8 @@ SIGNATURES = [
     ("spz_state_reset_zero", c_int, [c_void_p]),
     ("spz_state_copy", c_int, [c_void_p, c_void_p]),
     ("spz_state_fill_random", c_int, [c_void_p, c_uint64, c_int, c_int]),
+    ("spz_state_set_lazy", c_int, [c_void_p, c_int]),
+    ("spz_state_settle", c_int, [c_void_p]),
     ("spz_apply", c_int, [c_void_p, POINTER(spz_gate), c_uint32]),
     ("spz_c_apply", c_int, [c_void_p, POINTER(spz_gate), c_uint32, c_uint32]),
     ("spz_cc_apply", c_int, [c_void_p, POINTER(spz_gate), c_uint32, c_uint32, c_uint32]),

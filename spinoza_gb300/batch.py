@@ -69,14 +69,15 @@ class Batch:
     """A planned, device-resident batch; run(theta) -> (energies, grads)."""
 
     def __init__(self, instances: Sequence[Instance], tile_qubits: int = 0, threads: int = 0, wide_qubits: int = 0,
-                 fast: bool = False):
+                 fast: bool = False, tiles_per_item: int = 0):
         """tile_qubits / threads: launch shape of the persistent kernel;
-        wide_qubits: instances of at least this many qubits run one at a time
-        across the whole GPU (0: the library's default, 31: never); fast: those
-        use the fast adjoint (equal to the exact one up to rounding)."""
+        wide_qubits: instances of at least this many qubits are spread over
+        many CTAs as work items of tiles_per_item tiles (0: the library's
+        defaults, 31: never); fast: those run one at a time across the GPU with
+        the fast adjoint (equal to the exact one up to rounding)."""
         self.inst, self.ops, self.pidx, self.theta, self.terms = pack(instances)
         cfg = nat.spz_batch_config(int(tile_qubits), int(threads), int(wide_qubits),
-                                   nat.EXEC_FAST if fast else nat.EXEC_DEFAULT)
+                                   nat.EXEC_FAST if fast else nat.EXEC_DEFAULT, int(tiles_per_item))
         h = c_void_p()
         nat.check(nat.lib().spz_batch_create(nat.ptr(self.inst), len(self.inst), nat.ptr(self.ops),
                                              nat.ptr(self.pidx), nat.ptr(self.terms), byref(cfg), byref(h)))
@@ -112,7 +113,9 @@ class Batch:
             pass
 
 
-CANDIDATES = [(11, 128), (11, 256), (12, 256), (12, 512), (10, 128), (10, 64)]
+# (tile qubits, threads per CTA, tiles per work item of a wide instance)
+CANDIDATES = [(11, 128, 16), (11, 256, 16), (10, 128, 16), (10, 256, 16), (11, 128, 4), (11, 128, 64),
+              (12, 256, 16)]
 
 
 def _signature(instances: Sequence[Instance]) -> str:
@@ -127,9 +130,12 @@ def _cache_path() -> Path:
     return Path(base) / "batch_autotune.json"
 
 
-def autotune(instances: Sequence[Instance], candidates=CANDIDATES, reps: int = 1, use_cache: bool = True) -> dict:
-    """Pick (tile_qubits, threads) for this batch by timing each candidate; the
-    choice is cached per GPU name and batch signature."""
+def autotune(instances: Sequence[Instance], candidates=CANDIDATES, reps: int = 1, use_cache: bool = True,
+             sample: int = 512) -> dict:
+    """Pick (tile_qubits, threads, tiles_per_item) for this batch by timing
+    each candidate on a stratified sample of `sample` instances (every size and
+    depth represented); the choice is cached per GPU name and batch signature
+    (SPZ_AUTOTUNE_CACHE or ~/.cache/spinoza_gb300/batch_autotune.json)."""
     import torch
 
     key = f"{torch.cuda.get_device_name()}|{_signature(instances)}"
@@ -142,10 +148,13 @@ def autotune(instances: Sequence[Instance], candidates=CANDIDATES, reps: int = 1
             cache = {}
     if use_cache and key in cache:
         return cache[key]
+    order = sorted(range(len(instances)), key=lambda i: (instances[i][0], len(instances[i][1])))
+    step = max(1, len(order) // max(1, sample))
+    subset = [instances[i] for i in order[::step]]
     results = []
-    for k, t in candidates:
+    for k, t, tpi in candidates:
         try:
-            b = Batch(instances, tile_qubits=k, threads=t)
+            b = Batch(subset, tile_qubits=k, threads=t, tiles_per_item=tpi)
         except nat.SpzError:
             continue
         b.run()  # graph capture + warm-up
@@ -153,10 +162,10 @@ def autotune(instances: Sequence[Instance], candidates=CANDIDATES, reps: int = 1
         for _ in range(reps):
             b.run()
         dt = (time.perf_counter() - t0) / reps
-        results.append({"tile_qubits": k, "threads": t, "seconds": dt})
+        results.append({"tile_qubits": k, "threads": t, "tiles_per_item": tpi, "seconds": dt})
         b.close()
     best = min(results, key=lambda r: r["seconds"])
-    best = dict(best, candidates=results)
+    best = dict(best, candidates=results, sample=len(subset))
     if use_cache:
         cache[key] = best
         try:

@@ -128,6 +128,18 @@ class State:
     def synchronize(self) -> None:
         nat.check(nat.lib().spz_state_synchronize(self._h))
 
+    def set_lazy(self, enable: bool = True) -> None:
+        """Opt-in lazy per-gate arithmetic (spz_state_set_lazy): uncontrolled H,
+        RX, RY and RZ applied with half the FP64 work, a pending factor folded in
+        before any read; equal to the exact mode up to rounding.  States
+        wrapped around torch tensors must be settle()d before the tensors are
+        read directly."""
+        nat.check(nat.lib().spz_state_set_lazy(self._h, int(bool(enable))))
+
+    def settle(self) -> None:
+        """Fold the lazy mode's pending factor into the arrays now."""
+        nat.check(nat.lib().spz_state_settle(self._h))
+
     def set_stream(self, stream) -> None:
         """Issue this state's work on `stream`: a torch.cuda.Stream, a raw
         cudaStream_t as int, or None for the handle's own stream.  torch's

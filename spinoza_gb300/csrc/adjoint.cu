@@ -354,8 +354,8 @@ namespace {
 
 int ensure_aux(spz_state_t h, int j) {
   if (!h->aux_re[j]) {
-    SPZ_CUDA(cudaMalloc(&h->aux_re[j], h->N * sizeof(double)));
-    cudaError_t e = cudaMalloc(&h->aux_im[j], h->N * sizeof(double));
+    SPZ_CUDA(dev_alloc(&h->aux_re[j], h->N * sizeof(double)));
+    cudaError_t e = dev_alloc(&h->aux_im[j], h->N * sizeof(double));
     if (e != cudaSuccess) {
       cudaFree(h->aux_re[j]);
       h->aux_re[j] = nullptr;
@@ -720,5 +720,6 @@ extern "C" int spz_adjoint_gradient(spz_state_t h, const spz_op* ops, size_t nop
                                     size_t nparams, const spz_pauli_term* terms, size_t nterms, uint32_t flags,
                                     double* energy, double* grad) {
   if (!h) return fail(SPZ_ERR_NULL, "handle is NULL");
+  if (int rc = settle(h)) return rc;
   return adjoint_gradient(h, ops, nops, param_index, nparams, terms, nterms, flags, energy, grad, nullptr, nullptr);
 }

@@ -3,22 +3,34 @@
 // launch, replayed as a CUDA graph.  No reference counterpart (a new form built
 // on the gate path).
 //
-// Work split.  Each CTA takes whole instances from a global work counter
-// (largest first) and runs, for that instance:
+// Work split.  CTAs take work items from a global counter.  An item is either
+// a whole instance (smaller instances), run by one CTA:
 //   forward passes   psi = G_L ... G_1 |0>          (tiles of 2^k amplitudes)
 //   Hamiltonian      lam = H psi, E = Re<psi|lam>    (Pauli terms, tile passes)
 //   backward passes  per gate in reverse: the tile's part of <lam|K|psi>,
 //                    then G^dagger on both psi and lam (fused: one load of each)
+// or, for a wide instance (at least `wide_qubits` qubits), one pass of it over
+// a range of its tiles, so that one instance is spread over many CTAs.  A
+// wide instance's items of pass p wait until every item of its earlier passes
+// is complete (a per-instance completion counter), and the queue holds them
+// after all of those, so a waiting item only ever waits on items already
+// taken by running CTAs.  Each wait is bounded: past its limit the CTA sets
+// the batch's error flag and stops, every other CTA stops at its next item or
+// wait, and the run returns SPZ_ERR_TIMEOUT.  Wide items write their energy
+// and gradient partial sums to slots that a second kernel folds in a fixed
+// order.
+//
 // An instance of n <= k qubits lives entirely in shared memory (no HBM traffic
 // beyond parameters in and energy / gradients out).  Larger instances stream
-// tiles through a per-CTA workspace in HBM (psi and lam, 2 x 16 B x 2^n), using
-// the same planner as the fused circuit executor.  A CTA never waits on another
-// CTA, so there is no inter-CTA synchronisation to bound.
+// tiles through HBM workspace (psi and lam, 2 x 16 B x 2^n): per CTA for the
+// whole-instance items, per instance for the wide ones.
 //
-// Determinism: one CTA per instance, tiles in a fixed order, fixed reduction
-// trees: results are identical from run to run.
+// Determinism: fixed items, tiles in a fixed order within an item, fixed
+// reduction trees and partial-slot order: results are identical from run to
+// run.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <numeric>
 #include <vector>
@@ -46,6 +58,15 @@ constexpr int kDefaultWideQubits = 18;
 #define SPZ_BATCH_WIDE_STREAMS 3
 #endif
 constexpr int kWideStreams = SPZ_BATCH_WIDE_STREAMS;
+// Tiles per work item of a wide instance (2^11-amplitude tiles: 16 tiles of a
+// 22-qubit pass make 128 items).
+constexpr int kDefaultTilesPerItem = 16;
+// Polls (about 0.3 us each) before a dependency wait gives up: far longer
+// than any item takes, short enough that a lost dependency ends the launch.
+constexpr unsigned long long kDefaultWaitPolls = 1ull << 24;
+// HBM for the wide instances' own psi and lam: at most this share of the free
+// memory (the rest take the separate whole-GPU path).
+constexpr double kWideWorkspaceShare = 0.6;
 
 enum BPassKind { BP_FWD = 0, BP_HAM = 1, BP_BWD = 2 };
 enum BMode { BM_PAIR = 0, BM_DIAG_LOCAL = 1, BM_DIAG_GLOBAL = 2, BM_SWAP = 3 };
@@ -89,13 +110,35 @@ struct BInst {
   int32_t resident;   // n <= k: the whole instance stays in shared memory
   int64_t param_offset;
   int32_t nparams;
+  int32_t wide;       // >= 0: index of this wide instance (its completion counter); -1: whole-instance item
+  uint64_t ws_offset; // wide: psi_re, psi_im, lam_re, lam_im (2^n doubles each) from here in wide_ws
+};
+
+constexpr uint32_t kWholeInstance = 0xFFFFFFFFu;
+
+// One entry of the persistent kernel's queue.
+struct BItem {
+  uint32_t inst;
+  uint32_t pass;        // kWholeInstance, or the instance-relative pass this item runs
+  uint32_t need;        // wide: items of this instance that must be complete before this one starts
+  uint32_t slot;        // wide HAM / BWD: first partial-sum slot this item writes
+  uint64_t tile_begin, tile_end;
+};
+
+// Fold of partial-sum slots: out = factor * sum_{r < count} partials[base + r * stride].
+struct BSum {
+  uint64_t out;         // energies[out] (energy) or grads[out]
+  uint64_t base;
+  uint32_t stride, count;
+  double factor;
+  int32_t energy;
   int32_t pad;
 };
 
 struct BatchArgs {
   const BInst* inst;
-  const uint32_t* order;
-  uint32_t ninst;
+  const BItem* items;
+  uint32_t nitems;
   const BPass* passes;
   const BGate* gates;
   const HTerm* terms;
@@ -103,6 +146,11 @@ struct BatchArgs {
   double* grads;
   double* workspace;      // per CTA: psi_re, psi_im, lam_re, lam_im of 2^ws_qubits each
   uint32_t ws_qubits;
+  double* wide_ws;        // per wide instance (BInst::ws_offset)
+  unsigned int* done;     // per wide instance: completed items
+  double* partials;
+  int* error;             // 0, or 1 after a wait ran out
+  unsigned long long wait_limit;
   unsigned int* counter;
   int kmax;
 };
@@ -209,17 +257,183 @@ __device__ __forceinline__ uint64_t b_global(uint64_t base, const uint64_t* rowo
   return base | rowoff[e >> c] | (e & ((1u << c) - 1));
 }
 
+struct BSmem {
+  double *pr, *pi, *lr, *li;
+  uint64_t* rowoff;
+  double* red;
+  double* gacc;
+};
+
+// One pass of instance I over tiles [t0, t1): load each tile (or synthesise
+// |0...0>), apply the pass's work, store it back.  wpr .. wli: the instance's
+// psi and lam in HBM (unused when resident).  Energy terms add into *s_energy
+// (thread 0), gradient parts into S.gacc (zeroed here).  Workspace loads
+// bypass L1 (ld.global.cg): a wide instance's tiles are written by other CTAs.
+__device__ void run_pass(const BatchArgs& A, const BInst& I, const BPass& P, uint64_t t0, uint64_t t1, double* wpr,
+                         double* wpi, double* wlr, double* wli, const BSmem& S, double* s_energy) {
+  double* pr = S.pr;
+  double* pi = S.pi;
+  double* lr = S.lr;
+  double* li = S.li;
+  uint64_t* rowoff = S.rowoff;
+  const int K = P.k, C = P.c;
+  const uint32_t T = 1u << K;
+  if (!I.resident) {
+    for (uint32_t r = threadIdx.x; r < (1u << P.nhigh); r += blockDim.x) {
+      uint64_t off = 0;
+      for (int j = 0; j < P.nhigh; ++j)
+        if ((r >> j) & 1) off |= 1ull << P.lpos[C + j];
+      rowoff[r] = off;
+    }
+  }
+  if (P.kind == BP_BWD)
+    for (int j = threadIdx.x; j < P.nparams; j += blockDim.x) S.gacc[j] = 0.0;
+  __syncthreads();
+  for (uint64_t tile = t0; tile < t1; ++tile) {
+    const uint64_t base = I.resident ? 0 : deposit(tile, P.lpos, K);
+    // ---- load
+    if (P.kind == BP_FWD && P.first) {
+      for (uint32_t e = threadIdx.x; e < T; e += blockDim.x) {
+        const uint64_t gi = I.resident ? e : b_global(base, rowoff, e, C);
+        pr[e] = gi == 0 ? 1.0 : 0.0;
+        pi[e] = 0.0;
+      }
+    } else if (!I.resident) {
+      for (uint32_t e2 = threadIdx.x; e2 < T / 2; e2 += blockDim.x) {
+        const uint32_t e = 2 * e2;
+        const uint64_t gi = b_global(base, rowoff, e, C);
+        *reinterpret_cast<double2*>(pr + e) = __ldcg(reinterpret_cast<const double2*>(wpr + gi));
+        *reinterpret_cast<double2*>(pi + e) = __ldcg(reinterpret_cast<const double2*>(wpi + gi));
+        if (P.kind == BP_BWD || (P.kind == BP_HAM && !P.first)) {
+          *reinterpret_cast<double2*>(lr + e) = __ldcg(reinterpret_cast<const double2*>(wlr + gi));
+          *reinterpret_cast<double2*>(li + e) = __ldcg(reinterpret_cast<const double2*>(wli + gi));
+        }
+      }
+    }
+    __syncthreads();
+    // ---- work
+    if (P.kind == BP_FWD) {
+      for (uint32_t gi = 0; gi < P.gate_count; ++gi) {
+        const BGate& g = A.gates[P.gate_begin + gi];
+        if ((base & g.g_ones) != g.g_ones || (base & g.g_zeros) != 0) continue;
+        b_apply(g, base, pr, pi, T);
+        __syncthreads();
+      }
+    } else if (P.kind == BP_HAM) {
+      double eacc = 0.0;
+      for (uint32_t e = threadIdx.x; e < T; e += blockDim.x) {
+        const uint64_t gx = I.resident ? e : b_global(base, rowoff, e, C);
+        double dr = 0.0, di = 0.0;
+        for (uint32_t k = 0; k < P.term_count; ++k) {
+          const HTerm& h = A.terms[P.term_begin + k];
+          const uint32_t ye = e ^ (uint32_t)h.x_local;
+          const uint64_t gy = gx ^ h.x_global;
+          double cf = (__popcll(gy & h.z_mask) & 1) ? dneg(h.coeff) : h.coeff;
+          const int ny = h.ny & 3;
+          if (ny >= 2) cf = dneg(cf);
+          const double yr = pr[ye], yi = pi[ye];
+          if (ny & 1) {  // i * cf * psi_y
+            dr = dfma(dneg(cf), yi, dr);
+            di = dfma(cf, yr, di);
+          } else {
+            dr = dfma(cf, yr, dr);
+            di = dfma(cf, yi, di);
+          }
+        }
+        eacc = dadd(eacc, dfma(pr[e], dr, dmul(pi[e], di)));
+        if (P.first) {
+          lr[e] = dr;
+          li[e] = di;
+        } else {
+          lr[e] = dadd(lr[e], dr);
+          li[e] = dadd(li[e], di);
+        }
+      }
+      const double es = bsum(eacc, S.red);
+      if (threadIdx.x == 0) *s_energy = dadd(*s_energy, es);
+    } else {  // BP_BWD
+      for (uint32_t gi = 0; gi < P.gate_count; ++gi) {
+        const BGate& g = A.gates[P.gate_begin + gi];
+        if ((base & g.g_ones) != g.g_ones || (base & g.g_zeros) != 0) continue;
+        if (g.grad != BG_NONE) {
+          const double part = bsum(b_grad_part(g, base, pr, pi, lr, li, T), S.red);
+          if (threadIdx.x == 0) S.gacc[g.gacc] = dadd(S.gacc[g.gacc], part);
+        }
+        b_apply(g, base, pr, pi, T);
+        b_apply(g, base, lr, li, T);
+        __syncthreads();
+      }
+    }
+    __syncthreads();
+    // ---- store
+    if (!I.resident) {
+      const bool store_psi = P.kind != BP_HAM;
+      const bool store_lam = P.kind != BP_FWD;
+      for (uint32_t e2 = threadIdx.x; e2 < T / 2; e2 += blockDim.x) {
+        const uint32_t e = 2 * e2;
+        const uint64_t gi = b_global(base, rowoff, e, C);
+        if (store_psi) {
+          *reinterpret_cast<double2*>(wpr + gi) = *reinterpret_cast<const double2*>(pr + e);
+          *reinterpret_cast<double2*>(wpi + gi) = *reinterpret_cast<const double2*>(pi + e);
+        }
+        if (store_lam) {
+          *reinterpret_cast<double2*>(wlr + gi) = *reinterpret_cast<const double2*>(lr + e);
+          *reinterpret_cast<double2*>(wli + gi) = *reinterpret_cast<const double2*>(li + e);
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+__device__ __forceinline__ unsigned int ld_acquire_gpu(const unsigned int* p) {
+  unsigned int v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ int ld_volatile_int(const int* p) { return *reinterpret_cast<const volatile int*>(p); }
+
+// Thread 0 waits until *ctr >= need, at most A.wait_limit polls; returns false
+// (in every thread) on timeout, after setting the error flag, or when another
+// CTA already set it.
+__device__ bool wait_until(const BatchArgs& A, const unsigned int* ctr, unsigned int need, int* s_flag) {
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    unsigned long long polls = 0;
+    while (ld_acquire_gpu(ctr) < need) {
+      if (ld_volatile_int(A.error)) {
+        ok = 0;
+        break;
+      }
+      if (++polls > A.wait_limit) {
+        atomicCAS(A.error, 0, 1);
+        ok = 0;
+        break;
+      }
+      __nanosleep(256);
+    }
+    *s_flag = ok;
+  }
+  __syncthreads();
+  const bool ok = *s_flag != 0;
+  __syncthreads();
+  return ok;
+}
+
 __global__ void __launch_bounds__(1024) batch_kernel(BatchArgs A) {
   extern __shared__ double sm[];
   const uint32_t TMAX = 1u << A.kmax;
-  double* pr = sm;
-  double* pi = sm + TMAX;
-  double* lr = sm + 2 * TMAX;
-  double* li = sm + 3 * TMAX;
-  uint64_t* rowoff = reinterpret_cast<uint64_t*>(sm + 4 * TMAX);
-  double* red = sm + 4 * TMAX + (TMAX >> kBatchLowBits);
-  double* gacc = red + 64;
+  BSmem S;
+  S.pr = sm;
+  S.pi = sm + TMAX;
+  S.lr = sm + 2 * TMAX;
+  S.li = sm + 3 * TMAX;
+  S.rowoff = reinterpret_cast<uint64_t*>(sm + 4 * TMAX);
+  S.red = sm + 4 * TMAX + (TMAX >> kBatchLowBits);
+  S.gacc = S.red + 64;
   __shared__ unsigned int s_next;
+  __shared__ int s_flag;
   __shared__ double s_energy;
   const uint64_t wsN = 1ull << A.ws_qubits;
   double* wpr = A.workspace ? A.workspace + (uint64_t)blockIdx.x * 4 * wsN : nullptr;
@@ -228,139 +442,65 @@ __global__ void __launch_bounds__(1024) batch_kernel(BatchArgs A) {
   double* wli = wpr ? wpr + 3 * wsN : nullptr;
 
   for (;;) {
-    if (threadIdx.x == 0) s_next = atomicAdd(A.counter, 1u);
+    if (threadIdx.x == 0) s_next = ld_volatile_int(A.error) ? A.nitems : atomicAdd(A.counter, 1u);
     __syncthreads();
     const unsigned int q = s_next;
     __syncthreads();
-    if (q >= A.ninst) break;
-    const BInst I = A.inst[A.order[q]];
+    if (q >= A.nitems) break;
+    const BItem W = A.items[q];
+    const BInst I = A.inst[W.inst];
     if (threadIdx.x == 0) s_energy = 0.0;
     __syncthreads();
-    for (uint32_t pidx = 0; pidx < I.npass; ++pidx) {
-      const BPass& P = A.passes[I.pass_begin + pidx];
-      const int K = P.k, C = P.c;
-      const uint32_t T = 1u << K;
-      const uint64_t ntiles = 1ull << (I.n - K);
-      if (!I.resident) {
-        for (uint32_t r = threadIdx.x; r < (1u << P.nhigh); r += blockDim.x) {
-          uint64_t off = 0;
-          for (int j = 0; j < P.nhigh; ++j)
-            if ((r >> j) & 1) off |= 1ull << P.lpos[C + j];
-          rowoff[r] = off;
-        }
-      }
-      if (P.kind == BP_BWD)
-        for (int j = threadIdx.x; j < P.nparams; j += blockDim.x) gacc[j] = 0.0;
-      __syncthreads();
-      for (uint64_t tile = 0; tile < ntiles; ++tile) {
-        const uint64_t base = I.resident ? 0 : deposit(tile, P.lpos, K);
-        // ---- load
-        if (P.kind == BP_FWD && P.first) {
-          for (uint32_t e = threadIdx.x; e < T; e += blockDim.x) {
-            const uint64_t gi = I.resident ? e : b_global(base, rowoff, e, C);
-            pr[e] = gi == 0 ? 1.0 : 0.0;
-            pi[e] = 0.0;
-          }
-        } else if (!I.resident) {
-          for (uint32_t e2 = threadIdx.x; e2 < T / 2; e2 += blockDim.x) {
-            const uint32_t e = 2 * e2;
-            const uint64_t gi = b_global(base, rowoff, e, C);
-            *reinterpret_cast<double2*>(pr + e) = *reinterpret_cast<const double2*>(wpr + gi);
-            *reinterpret_cast<double2*>(pi + e) = *reinterpret_cast<const double2*>(wpi + gi);
-            if (P.kind == BP_BWD || (P.kind == BP_HAM && !P.first)) {
-              *reinterpret_cast<double2*>(lr + e) = *reinterpret_cast<const double2*>(wlr + gi);
-              *reinterpret_cast<double2*>(li + e) = *reinterpret_cast<const double2*>(wli + gi);
-            }
-          }
-        }
-        __syncthreads();
-        // ---- work
-        if (P.kind == BP_FWD) {
-          for (uint32_t gi = 0; gi < P.gate_count; ++gi) {
+    if (W.pass == kWholeInstance) {
+      for (uint32_t pidx = 0; pidx < I.npass; ++pidx) {
+        const BPass& P = A.passes[I.pass_begin + pidx];
+        run_pass(A, I, P, 0, 1ull << (I.n - P.k), wpr, wpi, wlr, wli, S, &s_energy);
+        if (P.kind == BP_BWD) {
+          for (uint32_t gi = threadIdx.x; gi < P.gate_count; gi += blockDim.x) {
             const BGate& g = A.gates[P.gate_begin + gi];
-            if ((base & g.g_ones) != g.g_ones || (base & g.g_zeros) != 0) continue;
-            b_apply(g, base, pr, pi, T);
-            __syncthreads();
-          }
-        } else if (P.kind == BP_HAM) {
-          double eacc = 0.0;
-          for (uint32_t e = threadIdx.x; e < T; e += blockDim.x) {
-            const uint64_t gx = I.resident ? e : b_global(base, rowoff, e, C);
-            double dr = 0.0, di = 0.0;
-            for (uint32_t k = 0; k < P.term_count; ++k) {
-              const HTerm& h = A.terms[P.term_begin + k];
-              const uint32_t ye = e ^ (uint32_t)h.x_local;
-              const uint64_t gy = gx ^ h.x_global;
-              double cf = (__popcll(gy & h.z_mask) & 1) ? dneg(h.coeff) : h.coeff;
-              const int ny = h.ny & 3;
-              if (ny >= 2) cf = dneg(cf);
-              const double yr = pr[ye], yi = pi[ye];
-              if (ny & 1) {  // i * cf * psi_y
-                dr = dfma(dneg(cf), yi, dr);
-                di = dfma(cf, yr, di);
-              } else {
-                dr = dfma(cf, yr, dr);
-                di = dfma(cf, yi, di);
-              }
-            }
-            eacc = dadd(eacc, dfma(pr[e], dr, dmul(pi[e], di)));
-            if (P.first) {
-              lr[e] = dr;
-              li[e] = di;
-            } else {
-              lr[e] = dadd(lr[e], dr);
-              li[e] = dadd(li[e], di);
-            }
-          }
-          const double es = bsum(eacc, red);
-          if (threadIdx.x == 0) s_energy = dadd(s_energy, es);
-        } else {  // BP_BWD
-          for (uint32_t gi = 0; gi < P.gate_count; ++gi) {
-            const BGate& g = A.gates[P.gate_begin + gi];
-            if ((base & g.g_ones) != g.g_ones || (base & g.g_zeros) != 0) continue;
             if (g.grad != BG_NONE) {
-              const double part = bsum(b_grad_part(g, base, pr, pi, lr, li, T), red);
-              if (threadIdx.x == 0) gacc[g.gacc] = dadd(gacc[g.gacc], part);
-            }
-            b_apply(g, base, pr, pi, T);
-            b_apply(g, base, lr, li, T);
-            __syncthreads();
-          }
-        }
-        __syncthreads();
-        // ---- store
-        if (!I.resident) {
-          const bool store_psi = P.kind != BP_HAM;
-          const bool store_lam = P.kind != BP_FWD;
-          for (uint32_t e2 = threadIdx.x; e2 < T / 2; e2 += blockDim.x) {
-            const uint32_t e = 2 * e2;
-            const uint64_t gi = b_global(base, rowoff, e, C);
-            if (store_psi) {
-              *reinterpret_cast<double2*>(wpr + gi) = *reinterpret_cast<const double2*>(pr + e);
-              *reinterpret_cast<double2*>(wpi + gi) = *reinterpret_cast<const double2*>(pi + e);
-            }
-            if (store_lam) {
-              *reinterpret_cast<double2*>(wlr + gi) = *reinterpret_cast<const double2*>(lr + e);
-              *reinterpret_cast<double2*>(wli + gi) = *reinterpret_cast<const double2*>(li + e);
+              const double v = S.gacc[g.gacc];
+              A.grads[I.param_offset + g.param] = g.grad == BG_P1 ? dmul(-2.0, v) : v;
             }
           }
+          __syncthreads();
         }
-        __syncthreads();
       }
-      if (P.kind == BP_BWD) {
-        for (uint32_t gi = threadIdx.x; gi < P.gate_count; gi += blockDim.x) {
-          const BGate& g = A.gates[P.gate_begin + gi];
-          if (g.grad != BG_NONE) {
-            const double v = gacc[g.gacc];
-            A.grads[I.param_offset + g.param] = g.grad == BG_P1 ? dmul(-2.0, v) : v;
-          }
-        }
-        __syncthreads();
-      }
+      if (threadIdx.x == 0) A.energies[W.inst] = s_energy;
+      __syncthreads();
+      continue;
     }
-    if (threadIdx.x == 0) A.energies[A.order[q]] = s_energy;
-    __syncthreads();
+    // one pass of a wide instance over a tile range
+    if (!wait_until(A, A.done + I.wide, W.need, &s_flag)) break;
+    const BPass& P = A.passes[I.pass_begin + W.pass];
+    const uint64_t N = 1ull << I.n;
+    double* ipr = A.wide_ws + I.ws_offset;
+    run_pass(A, I, P, W.tile_begin, W.tile_end, ipr, ipr + N, ipr + 2 * N, ipr + 3 * N, S, &s_energy);
+    if (P.kind == BP_HAM) {
+      if (threadIdx.x == 0) A.partials[W.slot] = s_energy;
+    } else if (P.kind == BP_BWD) {
+      for (int j = threadIdx.x; j < P.nparams; j += blockDim.x) A.partials[W.slot + j] = S.gacc[j];
+    }
+    __syncthreads();  // every thread's tile stores and partials are issued
+    if (threadIdx.x == 0) {
+      __threadfence();
+      atomicAdd(A.done + I.wide, 1u);
+    }
   }
+}
+
+// The wide instances' energies and gradients from their items' partial sums,
+// each a sequential sum in item order.
+__global__ void batch_fold_kernel(const BSum* __restrict__ sums, uint32_t nsums, const double* __restrict__ partials,
+                                  double* __restrict__ energies, double* __restrict__ grads) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nsums) return;
+  const BSum f = sums[i];
+  double v = 0.0;
+  for (uint32_t r = 0; r < f.count; ++r) v = dadd(v, partials[f.base + (uint64_t)r * f.stride]);
+  v = dmul(f.factor, v);
+  if (f.energy) energies[f.out] = v;
+  else grads[f.out] = v;
 }
 
 // Coefficients of every parameterised gate from the current angles.
@@ -491,9 +631,21 @@ struct BatchImpl {
   int grid = 0;
   size_t smem = 0;
   cudaStream_t stream = nullptr;
+  // wide instances inside the persistent kernel (work items)
+  int tiles_per_item = kDefaultTilesPerItem;
+  uint32_t nitems = 0, nwide_items = 0, nwide_in_kernel = 0, nsums = 0;
+  uint64_t npartials = 0, wide_ws_doubles = 0;
+  unsigned long long wait_limit = kDefaultWaitPolls;
+  bool stall_for_test = false;
   // device
   BInst* d_inst = nullptr;
-  uint32_t* d_order = nullptr;
+  BItem* d_items = nullptr;
+  BSum* d_sums = nullptr;
+  double* d_partials = nullptr;
+  double* d_wide_ws = nullptr;
+  unsigned int* d_done = nullptr;
+  int* d_error = nullptr;
+  int* h_error = nullptr;
   BPass* d_pass = nullptr;
   BGate* d_gates = nullptr;
   HTerm* d_terms = nullptr;
@@ -529,7 +681,9 @@ void free_batch(spz_batch_t b) {
     if (b->wide_done[si]) cudaEventDestroy(b->wide_done[si]);
     if (b->wide_stream[si]) cudaStreamDestroy(b->wide_stream[si]);
   }
-  cudaFree(b->d_inst); cudaFree(b->d_order); cudaFree(b->d_pass); cudaFree(b->d_gates); cudaFree(b->d_terms);
+  cudaFree(b->d_inst); cudaFree(b->d_items); cudaFree(b->d_sums); cudaFree(b->d_partials); cudaFree(b->d_wide_ws);
+  cudaFree(b->d_done); cudaFree(b->d_error); cudaFreeHost(b->h_error);
+  cudaFree(b->d_pass); cudaFree(b->d_gates); cudaFree(b->d_terms);
   cudaFree(b->d_jobs); cudaFree(b->d_theta); cudaFree(b->d_energy); cudaFree(b->d_grad); cudaFree(b->d_ws);
   cudaFree(b->d_counter);
   cudaFreeHost(b->h_theta); cudaFreeHost(b->h_energy); cudaFreeHost(b->h_grad);
@@ -540,7 +694,7 @@ void free_batch(spz_batch_t b) {
 template <typename T>
 int upload(T** dst, const std::vector<T>& src) {
   const size_t bytes = std::max<size_t>(1, src.size()) * sizeof(T);
-  SPZ_CUDA(cudaMalloc((void**)dst, bytes));
+  SPZ_CUDA(dev_alloc((void**)dst, bytes));
   if (!src.empty()) SPZ_CUDA(cudaMemcpy(*dst, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice));
   return SPZ_OK;
 }
@@ -555,12 +709,28 @@ int build_batch(spz_batch_t b, const spz_batch_instance* inst, size_t ninst, con
   std::vector<double> cost(ninst);
   uint64_t ptotal = 0;
   uint32_t ws_qubits = 0;
-  std::vector<uint32_t> narrow;
+  std::vector<uint32_t> narrow, wide_in;
+  std::vector<int32_t> wide_index(ninst, -1);
+  size_t free_b = 0, total_b = 0;
+  SPZ_CUDA(cudaMemGetInfo(&free_b, &total_b));
+  const uint64_t wide_budget = (uint64_t)(kWideWorkspaceShare * (double)free_b);
+  uint64_t wide_ws = 0;
   for (size_t ii = 0; ii < ninst; ++ii) {
     const spz_batch_instance& in = inst[ii];
     const uint32_t n = in.n;
     if (n == 0 || n > 30) return fail(SPZ_ERR_INVALID_ARGUMENT, "batch instance qubits must be in 1..30");
-    if ((int)n >= b->wide_qubits) {  // whole-GPU path: keep the instance's own lists
+    // Wide instances run as work items inside the persistent kernel, with
+    // their own psi and lam in HBM, when the workspace fits; the fast adjoint
+    // (SPZ_EXEC_FAST) and anything beyond the budget take the whole-GPU path.
+    const bool wide = (int)n >= b->wide_qubits && (int)n > b->kmax;
+    const uint64_t ws_need = 4ull * (1ull << n);
+    const bool in_kernel = wide && !(b->wide_flags & SPZ_EXEC_FAST) && (wide_ws + ws_need) * 8 <= wide_budget;
+    if (wide && in_kernel) {
+      wide_index[ii] = (int32_t)wide_in.size();
+      wide_in.push_back((uint32_t)ii);
+      wide_ws += ws_need;
+    }
+    if (wide && !in_kernel) {  // whole-GPU path: keep the instance's own lists
       WideInst w;
       w.idx = (uint32_t)ii;
       w.n = n;
@@ -582,7 +752,7 @@ int build_batch(spz_batch_t b, const spz_batch_instance* inst, size_t ninst, con
       b->wide.push_back(std::move(w));
       continue;
     }
-    narrow.push_back((uint32_t)ii);
+    if (!wide) narrow.push_back((uint32_t)ii);
     const int k = std::min<int>((int)n, b->kmax);
     const int c = std::min<int>(kBatchLowBits, k);
     // forward gate list (+ which op carries which parameter)
@@ -622,8 +792,9 @@ int build_batch(spz_batch_t b, const spz_batch_instance* inst, size_t ninst, con
     I.resident = (int)n <= b->kmax;
     I.param_offset = (int64_t)in.param_offset;
     I.nparams = (int)in.nparams;
+    I.wide = wide_index[ii];
     ptotal = std::max<uint64_t>(ptotal, in.param_offset + in.nparams);
-    if (!I.resident) ws_qubits = std::max<uint32_t>(ws_qubits, n);
+    if (!I.resident && I.wide < 0) ws_qubits = std::max<uint32_t>(ws_qubits, n);
     // forward passes (a resident instance is one pass over all n qubits, in program order)
     std::vector<int> all_local(n);
     std::iota(all_local.begin(), all_local.end(), 0);
@@ -786,23 +957,103 @@ int build_batch(spz_batch_t b, const spz_batch_instance* inst, size_t ninst, con
   std::vector<uint32_t> order = narrow;
   std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t c2) { return cost[a] > cost[c2]; });
   std::stable_sort(b->wide.begin(), b->wide.end(), [](const WideInst& a, const WideInst& c2) { return a.cost > c2.cost; });
+  // Queue: whole instances first, largest first (the longest single-CTA jobs
+  // start at once), then the wide instances' items pass by pass (pass p of
+  // every wide instance, largest instance first, before pass p + 1 of any),
+  // so that an item's dependencies sit far ahead of it in the queue.
+  std::vector<BItem> items;
+  for (uint32_t ii : order) items.push_back(BItem{ii, kWholeInstance, 0, 0, 0, 0});
+  std::vector<uint32_t> worder = wide_in;
+  std::stable_sort(worder.begin(), worder.end(), [&](uint32_t a, uint32_t c2) { return cost[a] > cost[c2]; });
+  // per wide instance: items per pass, partial-slot bases (contiguous per instance)
+  std::vector<BSum> sums;
+  std::vector<std::vector<uint32_t>> pass_items(ninst);
+  std::vector<std::vector<uint64_t>> pass_slot(ninst);
+  uint64_t nslots = 0;
+  uint32_t max_pass = 0;
+  const uint64_t tpi = (uint64_t)std::max(1, b->tiles_per_item);
+  uint64_t ws_off = 0;
+  for (uint32_t ii : worder) {
+    BInst& I = vinst[ii];
+    I.ws_offset = ws_off;
+    ws_off += 4ull * (1ull << I.n);
+    max_pass = std::max(max_pass, I.npass);
+    uint64_t ham_base = nslots, ham_count = 0;
+    for (uint32_t p = 0; p < I.npass; ++p) {  // HAM slots of the instance first, contiguous
+      const BPass& P = vpass[I.pass_begin + p];
+      const uint64_t ntiles = 1ull << (I.n - P.k);
+      const uint32_t m = (uint32_t)((ntiles + tpi - 1) / tpi);
+      pass_items[ii].push_back(m);
+      pass_slot[ii].push_back(0);
+      if (P.kind == BP_HAM) {
+        pass_slot[ii][p] = nslots;
+        nslots += m;
+        ham_count += m;
+      }
+    }
+    sums.push_back(BSum{ii, ham_base, 1, (uint32_t)ham_count, 1.0, 1, 0});
+    for (uint32_t p = 0; p < I.npass; ++p) {
+      const BPass& P = vpass[I.pass_begin + p];
+      if (P.kind != BP_BWD) continue;
+      pass_slot[ii][p] = nslots;
+      const uint32_t m = pass_items[ii][p];
+      for (uint32_t gi = 0; gi < P.gate_count; ++gi) {
+        const BGate& g = vgates[P.gate_begin + gi];
+        if (g.grad == BG_NONE) continue;
+        sums.push_back(BSum{(uint64_t)(I.param_offset + g.param), nslots + (uint64_t)g.gacc, (uint32_t)P.nparams, m,
+                            g.grad == BG_P1 ? -2.0 : 1.0, 0, 0});
+      }
+      nslots += (uint64_t)m * (uint64_t)P.nparams;
+    }
+  }
+  const uint32_t poison = 0xFFFFFFFFu;  // SPZ_BATCH_TEST_STALL: a count no item ever reaches
+  for (uint32_t p = 0; p < max_pass; ++p) {
+    for (uint32_t ii : worder) {
+      const BInst& I = vinst[ii];
+      if (p >= I.npass) continue;
+      const BPass& P = vpass[I.pass_begin + p];
+      const uint64_t ntiles = 1ull << (I.n - P.k);
+      uint32_t need = 0;
+      for (uint32_t q = 0; q < p; ++q) need += pass_items[ii][q];
+      if (b->stall_for_test && p > 0) need = poison;
+      const uint32_t m = pass_items[ii][p];
+      const uint32_t per_item = P.kind == BP_BWD ? (uint32_t)P.nparams : (P.kind == BP_HAM ? 1u : 0u);
+      for (uint32_t r = 0; r < m; ++r) {
+        const uint64_t t0 = (uint64_t)r * tpi, t1 = std::min<uint64_t>(ntiles, t0 + tpi);
+        items.push_back(BItem{ii, p, need, (uint32_t)(pass_slot[ii][p] + (uint64_t)r * per_item), t0, t1});
+      }
+    }
+  }
+  if (nslots >= 0xFFFFFFFFull) return fail(SPZ_ERR_UNSUPPORTED, "batch: too many partial-sum slots");
   b->ninst = (uint32_t)ninst;
   b->nnarrow = (uint32_t)narrow.size();
+  b->nitems = (uint32_t)items.size();
+  b->nwide_items = (uint32_t)(items.size() - order.size());
+  b->nwide_in_kernel = (uint32_t)wide_in.size();
+  b->nsums = (uint32_t)sums.size();
+  b->npartials = nslots;
+  b->wide_ws_doubles = ws_off;
   b->nparams_total = ptotal;
   b->ws_qubits = ws_qubits;
   b->njobs = (uint32_t)jobs.size();
   int rc;
-  if ((rc = upload(&b->d_inst, vinst)) || (rc = upload(&b->d_order, order)) || (rc = upload(&b->d_pass, vpass)) ||
-      (rc = upload(&b->d_gates, vgates)) || (rc = upload(&b->d_terms, vterms)) || (rc = upload(&b->d_jobs, jobs)))
+  if ((rc = upload(&b->d_inst, vinst)) || (rc = upload(&b->d_items, items)) || (rc = upload(&b->d_sums, sums)) ||
+      (rc = upload(&b->d_pass, vpass)) || (rc = upload(&b->d_gates, vgates)) || (rc = upload(&b->d_terms, vterms)) ||
+      (rc = upload(&b->d_jobs, jobs)))
     return rc;
-  SPZ_CUDA(cudaMalloc(&b->d_theta, std::max<uint64_t>(1, ptotal) * sizeof(double)));
-  SPZ_CUDA(cudaMalloc(&b->d_grad, std::max<uint64_t>(1, ptotal) * sizeof(double)));
-  SPZ_CUDA(cudaMalloc(&b->d_energy, std::max<size_t>(1, ninst) * sizeof(double)));
-  SPZ_CUDA(cudaMalloc(&b->d_counter, sizeof(unsigned int)));
+  SPZ_CUDA(dev_alloc(&b->d_partials, std::max<uint64_t>(1, nslots) * sizeof(double)));
+  SPZ_CUDA(dev_alloc(&b->d_done, std::max<size_t>(1, wide_in.size()) * sizeof(unsigned int)));
+  SPZ_CUDA(dev_alloc(&b->d_error, sizeof(int)));
+  SPZ_CUDA(host_alloc(&b->h_error, sizeof(int)));
+  if (ws_off) SPZ_CUDA(dev_alloc(&b->d_wide_ws, ws_off * sizeof(double)));
+  SPZ_CUDA(dev_alloc(&b->d_theta, std::max<uint64_t>(1, ptotal) * sizeof(double)));
+  SPZ_CUDA(dev_alloc(&b->d_grad, std::max<uint64_t>(1, ptotal) * sizeof(double)));
+  SPZ_CUDA(dev_alloc(&b->d_energy, std::max<size_t>(1, ninst) * sizeof(double)));
+  SPZ_CUDA(dev_alloc(&b->d_counter, sizeof(unsigned int)));
   SPZ_CUDA(cudaMemset(b->d_grad, 0, std::max<uint64_t>(1, ptotal) * sizeof(double)));
-  SPZ_CUDA(cudaMallocHost(&b->h_theta, std::max<uint64_t>(1, ptotal) * sizeof(double)));
-  SPZ_CUDA(cudaMallocHost(&b->h_grad, std::max<uint64_t>(1, ptotal) * sizeof(double)));
-  SPZ_CUDA(cudaMallocHost(&b->h_energy, std::max<size_t>(1, ninst) * sizeof(double)));
+  SPZ_CUDA(host_alloc(&b->h_theta, std::max<uint64_t>(1, ptotal) * sizeof(double)));
+  SPZ_CUDA(host_alloc(&b->h_grad, std::max<uint64_t>(1, ptotal) * sizeof(double)));
+  SPZ_CUDA(host_alloc(&b->h_energy, std::max<size_t>(1, ninst) * sizeof(double)));
   // launch shape: persistent CTAs, as many per SM as shared memory allows
   const uint32_t TMAX = 1u << b->kmax;
   b->smem = (4 * TMAX + (TMAX >> kBatchLowBits) + 64 + kMaxPassParams) * sizeof(double);
@@ -812,19 +1063,18 @@ int build_batch(spz_batch_t b, const spz_batch_instance* inst, size_t ninst, con
   if (per_sm < 1) return fail(SPZ_ERR_UNSUPPORTED, "batch kernel does not fit on an SM with this configuration");
   int sms = 0;
   SPZ_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device));
-  b->grid = std::max(1, std::min<int>(sms * per_sm, (int)b->nnarrow));
+  b->grid = std::max(1, std::min<int>(sms * per_sm, (int)b->nitems));
   if (ws_qubits) {
     // Each CTA owns psi and lam of the largest streamed instance; keep the
     // workspace within half of the free device memory, at most
     // kWorkspaceBudget (and at least one CTA per SM).
-    size_t free_b = 0, total_b = 0;
     SPZ_CUDA(cudaMemGetInfo(&free_b, &total_b));
     const uint64_t budget = std::min<uint64_t>(kWorkspaceBudget, free_b / 2);
     const uint64_t per_cta = 4ull * (1ull << ws_qubits) * sizeof(double);
     const uint64_t cap = std::max<uint64_t>((uint64_t)sms, budget / per_cta);
     b->grid = (int)std::min<uint64_t>((uint64_t)b->grid, cap);
     const size_t bytes = (size_t)b->grid * 4 * (1ull << ws_qubits) * sizeof(double);
-    SPZ_CUDA(cudaMalloc(&b->d_ws, bytes));
+    SPZ_CUDA(dev_alloc(&b->d_ws, bytes));
   }
   return SPZ_OK;
 }
@@ -835,11 +1085,18 @@ int capture_graph(spz_batch_t b) {
   cudaMemcpyAsync(b->d_theta, b->h_theta, std::max<uint64_t>(1, b->nparams_total) * sizeof(double),
                   cudaMemcpyHostToDevice, b->stream);
   cudaMemsetAsync(b->d_counter, 0, sizeof(unsigned int), b->stream);
+  cudaMemsetAsync(b->d_done, 0, std::max<size_t>(1, b->nwide_in_kernel) * sizeof(unsigned int), b->stream);
+  cudaMemsetAsync(b->d_error, 0, sizeof(int), b->stream);
   if (b->njobs) batch_coef_kernel<<<(b->njobs + 255) / 256, 256, 0, b->stream>>>(b->d_gates, b->d_jobs, b->njobs, b->d_theta);
   BatchArgs A{};
   A.inst = b->d_inst;
-  A.order = b->d_order;
-  A.ninst = b->nnarrow;
+  A.items = b->d_items;
+  A.nitems = b->nitems;
+  A.wide_ws = b->d_wide_ws;
+  A.done = b->d_done;
+  A.partials = b->d_partials;
+  A.error = b->d_error;
+  A.wait_limit = b->wait_limit;
   A.passes = b->d_pass;
   A.gates = b->d_gates;
   A.terms = b->d_terms;
@@ -849,7 +1106,11 @@ int capture_graph(spz_batch_t b) {
   A.ws_qubits = b->ws_qubits;
   A.counter = b->d_counter;
   A.kmax = b->kmax;
-  if (b->nnarrow) batch_kernel<<<b->grid, b->threads, b->smem, b->stream>>>(A);
+  if (b->nitems) batch_kernel<<<b->grid, b->threads, b->smem, b->stream>>>(A);
+  if (b->nsums)
+    batch_fold_kernel<<<(b->nsums + 255) / 256, 256, 0, b->stream>>>(b->d_sums, b->nsums, b->d_partials, b->d_energy,
+                                                                     b->d_grad);
+  cudaMemcpyAsync(b->h_error, b->d_error, sizeof(int), cudaMemcpyDeviceToHost, b->stream);
   cudaError_t e = cudaStreamEndCapture(b->stream, &g);
   if (e != cudaSuccess) return cuda_fail(e, "batch graph capture");
   e = cudaGraphInstantiate(&b->graph, g, 0);
@@ -876,6 +1137,18 @@ int spz_batch_create(const spz_batch_instance* instances, size_t ninstances, con
     if (config->threads) b->threads = config->threads;
     if (config->wide_qubits) b->wide_qubits = config->wide_qubits;
     b->wide_flags = (uint32_t)config->flags & SPZ_EXEC_FAST;
+    if (config->tiles_per_item) b->tiles_per_item = config->tiles_per_item;
+  }
+  {  // host-side fault injection for tests: wide items wait on counts never reached
+    const char* v = std::getenv("SPZ_BATCH_TEST_STALL");
+    if (v && v[0] == '1' && v[1] == 0) {
+      b->stall_for_test = true;
+      b->wait_limit = 4096;
+    }
+  }
+  if (b->tiles_per_item < 1) {
+    delete b;
+    return fail(SPZ_ERR_INVALID_ARGUMENT, "batch config: tiles_per_item must be >= 1");
   }
   if (b->kmax < 4 || b->kmax > kBatchMaxK || b->threads < 64 || b->threads > 1024 || (b->threads & 31)) {
     delete b;
@@ -949,6 +1222,9 @@ int spz_batch_run(spz_batch_t b, const double* theta, double* energies, double* 
   SPZ_CUDA(cudaMemcpyAsync(b->h_grad, b->d_grad, std::max<uint64_t>(1, b->nparams_total) * sizeof(double),
                            cudaMemcpyDeviceToHost, b->stream));
   SPZ_CUDA(cudaStreamSynchronize(b->stream));
+  if (*b->h_error)
+    return fail(SPZ_ERR_TIMEOUT, "batch: a work item's dependency wait ran out; the launch stopped early and its "
+                                 "outputs are incomplete");
   std::memcpy(energies, b->h_energy, b->ninst * sizeof(double));
   if (b->nparams_total) std::memcpy(grads, b->h_grad, b->nparams_total * sizeof(double));
   return SPZ_OK;
@@ -965,6 +1241,11 @@ int spz_batch_info(spz_batch_t b, spz_batch_stats* st) {
   st->workspace_bytes = b->ws_qubits ? (uint64_t)b->grid * 4 * (1ull << b->ws_qubits) * sizeof(double) : 0;
   st->tile_qubits = b->kmax;
   st->threads = b->threads;
+  st->wide_in_kernel = b->nwide_in_kernel;
+  st->work_items = b->nitems;
+  st->wide_separate = b->wide.size();
+  st->wide_workspace_bytes = b->wide_ws_doubles * sizeof(double);
+  st->tiles_per_item = b->tiles_per_item;
   return SPZ_OK;
 }
 

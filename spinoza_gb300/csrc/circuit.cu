@@ -1236,7 +1236,7 @@ int build_program(spz_program_t p, const spz_op* ops, size_t nops, uint32_t flag
   const size_t gbytes = (all.size() * sizeof(TileGate) + 255) / 256 * 256;
   const size_t tbytes = flat.size() * sizeof(double);
   if (gbytes + tbytes) {
-    SPZ_CUDA(cudaMalloc(&p->dbuf, gbytes + tbytes));
+    SPZ_CUDA(dev_alloc(&p->dbuf, gbytes + tbytes));
     if (!all.empty())
       SPZ_CUDA(cudaMemcpy(p->dbuf, all.data(), all.size() * sizeof(TileGate), cudaMemcpyHostToDevice));
     if (tbytes) SPZ_CUDA(cudaMemcpy((char*)p->dbuf + gbytes, flat.data(), tbytes, cudaMemcpyHostToDevice));
@@ -1335,6 +1335,7 @@ int spz_circuit_execute(spz_state_t h, const spz_op* ops, size_t nops, spz_track
   if (!h) return fail(SPZ_ERR_NULL, "handle is NULL");
   if (nops && !ops) return fail(SPZ_ERR_NULL, "ops is NULL");
   if (stats) std::memset(stats, 0, sizeof(*stats));
+  if (int rc = settle(h)) return rc;  // measurements read the state
   return execute(h, ops, nops, tracker, flags, stats);
 }
 
@@ -1344,6 +1345,7 @@ int spz_circuit_execute_host(spz_state_t h, const double* in_reals, const double
   if (!h || !in_reals || !in_imags || !out_reals || !out_imags) return fail(SPZ_ERR_NULL, "NULL argument");
   if (nops && !ops) return fail(SPZ_ERR_NULL, "ops is NULL");
   if (stats) std::memset(stats, 0, sizeof(*stats));
+  clear_factor(h);  // the handle's contents are replaced by the input arrays
   auto pinned = [](const void* p) {
     cudaPointerAttributes a{};
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {

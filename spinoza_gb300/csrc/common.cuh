@@ -38,6 +38,19 @@ int cuda_fail(cudaError_t e, const char* what);
     if (e_ != cudaSuccess) return ::spz::cuda_fail(e_, what); \
   } while (0)
 
+// ------------------------------------------------------------ allocation
+// Every device and page-locked host allocation of the library goes through
+// these two.  While the environment variable SPZ_INJECT_ALLOC_FAILURE is set
+// to 1 they return cudaErrorMemoryAllocation without allocating: a host-side
+// fault injection that exercises the out-of-memory paths (the call returns
+// SPZ_ERR_OUT_OF_MEMORY and leaves its handle usable) with no GPU fault.
+cudaError_t dev_alloc(void** p, size_t bytes);
+cudaError_t host_alloc(void** p, size_t bytes);
+template <class T>
+inline cudaError_t dev_alloc(T** p, size_t bytes) { return dev_alloc(reinterpret_cast<void**>(p), bytes); }
+template <class T>
+inline cudaError_t host_alloc(T** p, size_t bytes) { return host_alloc(reinterpret_cast<void**>(p), bytes); }
+
 // ------------------------------------------------------------ the handle
 struct Scratch {
   void* ptr = nullptr;
@@ -67,11 +80,23 @@ struct spz_state_s {
   // Measurements made inside the executor, kept on the device (lazily
   // allocated): prob0[64], scale[64] (doubles), then outcome[64] (int32).
   double* meas = nullptr;
+  // Lazy per-gate mode (spz_state_set_lazy): the state is
+  // (factor_re + i factor_im) * 2^factor_exp * (re, im); the factor is folded
+  // into the arrays (settle) before anything reads them.
+  bool lazy = false;
+  double factor_re = 1.0, factor_im = 0.0;
+  int factor_exp = 0;
 };
 
 namespace spz {
 
 int ensure_dev_scratch(spz_state_t h, size_t bytes, void** out);
+// Lazy per-gate mode (state.cu): fold a pending factor into the arrays (one
+// scaling pass, nothing when the factor is 1); forget it (the arrays were
+// overwritten); multiply it by f.
+int settle(spz_state_t h);
+void clear_factor(spz_state_t h);
+int scale_factor(spz_state_t h, double f_re, double f_im);
 int ensure_host_scratch(spz_state_t h, size_t bytes, void** out);
 int grid_for(uint64_t work, int threads = kThreads, int per_sm = 16);
 

@@ -168,6 +168,14 @@ struct PairArgs {
   uint8_t pos[kMaxQubits + 2];
 };
 
+// Exact gates use the reference's arithmetic; the lazy kinds (FK_LAZY_*, the
+// gate divided by a scalar) use the 4-instruction forms.
+template <int KIND>
+__device__ __forceinline__ void pair_op(const Coef& c, double& a, double& b, double& x, double& d) {
+  if constexpr (KIND >= FK_LAZY_H) fast_pair<KIND>(c, a, b, x, d);
+  else gate_pair<KIND>(c, a, b, x, d);
+}
+
 // Two consecutive pairs per thread; requires every special position >= 1.
 template <int KIND>
 __global__ void __launch_bounds__(kThreads) pair_kernel_v2(PairArgs A) {
@@ -179,8 +187,8 @@ __global__ void __launch_bounds__(kThreads) pair_kernel_v2(PairArgs A) {
     double2 i0 = *reinterpret_cast<const double2*>(A.im + s0);
     double2 r1 = *reinterpret_cast<const double2*>(A.re + s1);
     double2 i1 = *reinterpret_cast<const double2*>(A.im + s1);
-    gate_pair<KIND>(A.c, r0.x, i0.x, r1.x, i1.x);
-    gate_pair<KIND>(A.c, r0.y, i0.y, r1.y, i1.y);
+    pair_op<KIND>(A.c, r0.x, i0.x, r1.x, i1.x);
+    pair_op<KIND>(A.c, r0.y, i0.y, r1.y, i1.y);
     *reinterpret_cast<double2*>(A.re + s0) = r0;
     *reinterpret_cast<double2*>(A.im + s0) = i0;
     *reinterpret_cast<double2*>(A.re + s1) = r1;
@@ -196,7 +204,7 @@ __global__ void __launch_bounds__(kThreads) pair_kernel_t0(PairArgs A) {
     const uint64_t s0 = deposit(w, A.pos, A.npos) | A.ones;
     double2 r = *reinterpret_cast<const double2*>(A.re + s0);
     double2 i = *reinterpret_cast<const double2*>(A.im + s0);
-    gate_pair<KIND>(A.c, r.x, i.x, r.y, i.y);
+    pair_op<KIND>(A.c, r.x, i.x, r.y, i.y);
     *reinterpret_cast<double2*>(A.re + s0) = r;
     *reinterpret_cast<double2*>(A.im + s0) = i;
   }
@@ -210,7 +218,7 @@ __global__ void __launch_bounds__(kThreads) pair_kernel_s(PairArgs A) {
     const uint64_t s0 = deposit(w, A.pos, A.npos) | A.ones;
     const uint64_t s1 = s0 | A.tbit;
     double a = A.re[s0], b = A.im[s0], c = A.re[s1], d = A.im[s1];
-    gate_pair<KIND>(A.c, a, b, c, d);
+    pair_op<KIND>(A.c, a, b, c, d);
     A.re[s0] = a;
     A.im[s0] = b;
     A.re[s1] = c;
@@ -376,9 +384,69 @@ int launch_gate(spz_state_t h, const GateApp& g) {
   }
 }
 
+// Lazy per-gate mode (opt-in, spz_state_set_lazy): uncontrolled H, RX and RY
+// are applied as the gate divided by a real scalar (1/sqrt 2, or the larger
+// in magnitude of cos and sin of theta/2, so the remaining coefficient is at
+// most 1): 4 FP64 instructions per pair instead of 8-12, which makes them
+// bound by HBM.  RZ(theta) = e^{-i theta/2} P(theta): P touches only the 1
+// half.  The scalars and phases multiply the handle's pending factor.  Sets
+// *done when the gate was applied here.
+int apply_lazy(spz_state_t h, const spz_gate& gate, uint32_t target, bool* done) {
+  *done = false;
+  const int k = gate.kind;
+  if (k != SPZ_GATE_H && k != SPZ_GATE_RX && k != SPZ_GATE_RY && k != SPZ_GATE_RZ) return SPZ_OK;
+  GateApp a;
+  int rc = make_gate_app(h->n, gate, target, 0, 0, &a);
+  if (rc) return rc;
+  PairArgs A{};
+  A.re = h->re;
+  A.im = h->im;
+  const uint64_t tbit = 1ull << target;
+  A.tbit = tbit;
+  if (k == SPZ_GATE_RZ) {
+    spz_gate p{};
+    p.kind = SPZ_GATE_P;
+    p.p[0] = gate.p[0];
+    rc = coef_for(p, &A.c);
+    if (rc) return rc;
+    A.ones = tbit;
+    fill_positions(A, tbit);
+    rc = launch_diag<SPZ_GATE_P>(h, A, tbit);
+    if (rc) return rc;
+    *done = true;
+    return scale_factor(h, a.c.d0re, a.c.d0im);
+  }
+  fill_positions(A, tbit);
+  double f;
+  if (k == SPZ_GATE_H) {
+    rc = launch_pair<FK_LAZY_H>(h, A, tbit);
+    f = std::sqrt(0.5);
+  } else {
+    const double c = a.c.cs, sn = a.c.sn;
+    const bool x = k == SPZ_GATE_RX;
+    if (std::fabs(c) >= std::fabs(sn)) {
+      A.c.cs = sn / c;
+      rc = x ? launch_pair<FK_LAZY_RX_A>(h, A, tbit) : launch_pair<FK_LAZY_RY_A>(h, A, tbit);
+      f = c;
+    } else {
+      A.c.cs = c / sn;
+      rc = x ? launch_pair<FK_LAZY_RX_B>(h, A, tbit) : launch_pair<FK_LAZY_RY_B>(h, A, tbit);
+      f = sn;
+    }
+  }
+  if (rc) return rc;
+  *done = true;
+  return scale_factor(h, f, 0.0);
+}
+
 // Apply one gate under controls, with BitFlipNoise resolved on the host.
 int apply_controlled(spz_state_t h, const spz_gate* gate, uint32_t target, uint64_t ones, uint64_t zeros) {
   if (!h || !gate) return fail(SPZ_ERR_NULL, "NULL argument");
+  if (h->lazy && ones == 0 && zeros == 0) {
+    bool done = false;
+    int rc = apply_lazy(h, *gate, target, &done);
+    if (rc || done) return rc;
+  }
   if (gate->kind == SPZ_GATE_BITFLIP) {
     if (target >= h->n) return fail(SPZ_ERR_INVALID_ARGUMENT, "target qubit out of range");
     if (!(gate->p[1] <= gate->p[0])) return SPZ_OK;  // gates.rs:1369: X iff epsilon <= prob

@@ -26,7 +26,7 @@ extern "C" int spz_probe_fp64_fma_rate(double* fma_per_s) {
   SPZ_CUDA(cudaGetDevice(&dev));
   SPZ_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   double* d;
-  SPZ_CUDA(cudaMalloc(&d, 64));
+  SPZ_CUDA(dev_alloc(&d, 64));
   cudaEvent_t e0, e1;
   SPZ_CUDA(cudaEventCreate(&e0));
   SPZ_CUDA(cudaEventCreate(&e1));

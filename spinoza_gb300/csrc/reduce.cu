@@ -187,7 +187,7 @@ __global__ void collapse_meas_kernel(double* __restrict__ re, double* __restrict
 int measure_on_device(spz_state_t h, uint32_t target, int reset, double u) {
   if (target >= h->n) return fail(SPZ_ERR_INVALID_ARGUMENT, "target qubit out of range");
   if (!h->meas) {
-    SPZ_CUDA(cudaMalloc(&h->meas, (kMeasOutcomeOffset + 64) * sizeof(double)));
+    SPZ_CUDA(dev_alloc(&h->meas, (kMeasOutcomeOffset + 64) * sizeof(double)));
     SPZ_CUDA(cudaMemsetAsync(h->meas, 0, (kMeasOutcomeOffset + 64) * sizeof(double), h->stream));
   }
   void* scratch;
@@ -862,6 +862,7 @@ extern "C" {
 
 int spz_prob0(spz_state_t h, uint32_t target, double* prob0) {
   if (!h || !prob0) return fail(SPZ_ERR_NULL, "NULL argument");
+  if (int rc0 = settle(h)) return rc0;
   if (target >= h->n) return fail(SPZ_ERR_INVALID_ARGUMENT, "target qubit out of range");
   return prob0_device(h, target, prob0);
 }
@@ -869,11 +870,13 @@ int spz_prob0(spz_state_t h, uint32_t target, double* prob0) {
 int spz_measure_qubit(spz_state_t h, uint32_t target, int reset, int forced, double u, uint8_t* outcome,
                       double* prob0) {
   if (!h || !outcome) return fail(SPZ_ERR_NULL, "NULL argument");
+  if (int rc0 = settle(h)) return rc0;
   return measure_qubit(h, target, reset, forced, u, outcome, prob0);
 }
 
 int spz_qubit_expectation_value(spz_state_t h, uint32_t target, double* out) {
   if (!h || !out) return fail(SPZ_ERR_NULL, "NULL argument");
+  if (int rc0 = settle(h)) return rc0;
   if (target >= h->n) return fail(SPZ_ERR_INVALID_ARGUMENT, "target qubit out of range");
   double p0;
   int rc = prob0_device(h, target, &p0);
@@ -885,6 +888,7 @@ int spz_qubit_expectation_value(spz_state_t h, uint32_t target, double* out) {
 int spz_xyz_expectation_value(spz_state_t h, char observable, const uint32_t* targets, uint32_t ntargets,
                               double* out) {
   if (!h || (ntargets && (!targets || !out))) return fail(SPZ_ERR_NULL, "NULL argument");
+  if (int rc0 = settle(h)) return rc0;
   int mode;
   switch (observable) {
     case 'x': mode = RED_X; break;
@@ -903,16 +907,19 @@ int spz_xyz_expectation_value(spz_state_t h, char observable, const uint32_t* ta
 
 int spz_pauli_expectation(spz_state_t h, const spz_pauli_term* terms, size_t nterms, double* out) {
   if (!h || !out) return fail(SPZ_ERR_NULL, "NULL argument");
+  if (int rc0 = settle(h)) return rc0;
   return pauli_expectation(h, terms, nterms, out);
 }
 
 int spz_norm_sqr(spz_state_t h, double* out) {
   if (!h || !out) return fail(SPZ_ERR_NULL, "NULL argument");
+  if (int rc0 = settle(h)) return rc0;
   return reduce_scalar(h, RED_NORM, 0, out);
 }
 
 int spz_sample(spz_state_t h, const double* u, size_t nshots, uint64_t* out) {
   if (!h) return fail(SPZ_ERR_NULL, "handle is NULL");
+  if (int rc0 = settle(h)) return rc0;
   return sample(h, u, nshots, out);
 }
 

@@ -1,8 +1,10 @@
 // State handles: allocation, wrapping of caller memory, host<->device copies,
 // reset, clone and seeded synthetic fills.  Replaces State::new / Clone and the
 // public reals/imags fields of spinoza/src/core.rs:18-51.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -27,6 +29,23 @@ int cuda_fail(cudaError_t e, const char* what) {
   return e == cudaErrorMemoryAllocation ? SPZ_ERR_OUT_OF_MEMORY : SPZ_ERR_CUDA;
 }
 
+namespace {
+bool alloc_failure_injected() {
+  const char* v = std::getenv("SPZ_INJECT_ALLOC_FAILURE");
+  return v && v[0] == '1' && v[1] == 0;
+}
+}  // namespace
+
+cudaError_t dev_alloc(void** p, size_t bytes) {
+  if (alloc_failure_injected()) return cudaErrorMemoryAllocation;
+  return cudaMalloc(p, bytes);
+}
+
+cudaError_t host_alloc(void** p, size_t bytes) {
+  if (alloc_failure_injected()) return cudaErrorMemoryAllocation;
+  return cudaMallocHost(p, bytes);
+}
+
 int grid_for(uint64_t work, int threads, int per_sm) {
   uint64_t blocks = (work + threads - 1) / threads;
   uint64_t cap = (uint64_t)kNumSMs * per_sm;
@@ -44,7 +63,7 @@ int ensure_dev_scratch(spz_state_t h, size_t bytes, void** out) {
       h->dev_scratch.bytes = 0;
     }
     size_t sz = bytes < 4096 ? 4096 : bytes;
-    SPZ_CUDA(cudaMalloc(&h->dev_scratch.ptr, sz));
+    SPZ_CUDA(dev_alloc(&h->dev_scratch.ptr, sz));
     h->dev_scratch.bytes = sz;
   }
   *out = h->dev_scratch.ptr;
@@ -60,7 +79,7 @@ int ensure_host_scratch(spz_state_t h, size_t bytes, void** out) {
       h->host_scratch.bytes = 0;
     }
     size_t sz = bytes < 4096 ? 4096 : bytes;
-    SPZ_CUDA(cudaMallocHost(&h->host_scratch.ptr, sz));
+    SPZ_CUDA(host_alloc(&h->host_scratch.ptr, sz));
     h->host_scratch.bytes = sz;
   }
   *out = h->host_scratch.ptr;
@@ -120,6 +139,65 @@ __global__ void scale_kernel(double* __restrict__ re, double* __restrict__ im, u
 
 __global__ void rsqrt_kernel(double* p) { p[1] = 1.0 / sqrt(p[0]); }
 
+// Multiply every amplitude by the complex factor (fr, fi); a real factor
+// (fi == 0) costs one multiply per number.  Two amplitudes per thread
+// (double2 loads), so the pass is bound by HBM.
+__global__ void __launch_bounds__(kThreads) factor_kernel(double* __restrict__ re, double* __restrict__ im,
+                                                          uint64_t npairs, double fr, double fi) {
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < npairs; w += stride) {
+    double2 r = reinterpret_cast<const double2*>(re)[w];
+    double2 i = reinterpret_cast<const double2*>(im)[w];
+    if (fi == 0.0) {
+      r.x = dmul(r.x, fr); r.y = dmul(r.y, fr);
+      i.x = dmul(i.x, fr); i.y = dmul(i.y, fr);
+    } else {
+      const double ax = r.x, bx = i.x, ay = r.y, by = i.y;
+      r.x = dfma(ax, fr, dmul(dneg(bx), fi)); i.x = dfma(ax, fi, dmul(bx, fr));
+      r.y = dfma(ay, fr, dmul(dneg(by), fi)); i.y = dfma(ay, fi, dmul(by, fr));
+    }
+    reinterpret_cast<double2*>(re)[w] = r;
+    reinterpret_cast<double2*>(im)[w] = i;
+  }
+}
+
+void clear_factor(spz_state_t h) {
+  h->factor_re = 1.0;
+  h->factor_im = 0.0;
+  h->factor_exp = 0;
+}
+
+int settle(spz_state_t h) {
+  if (h->factor_re == 1.0 && h->factor_im == 0.0 && h->factor_exp == 0) return SPZ_OK;
+  const double fr = std::ldexp(h->factor_re, h->factor_exp), fi = std::ldexp(h->factor_im, h->factor_exp);
+  clear_factor(h);
+  if (h->N >= 2) {
+    factor_kernel<<<grid_for(h->N / 2), kThreads, 0, h->stream>>>(h->re, h->im, h->N / 2, fr, fi);
+  } else {
+    return fail(SPZ_ERR_INVALID_ARGUMENT, "state too small");
+  }
+  SPZ_CHECK_LAUNCH("factor_kernel");
+  return SPZ_OK;
+}
+
+// The arrays hold the state divided by the factor; a lazy gate that applies
+// (its matrix / f) multiplies the factor by f.  The factor is kept as
+// mantissa x 2^exp; once the arrays have grown by 2^400 (each lazy gate grows
+// them by at most sqrt 2) the factor is folded in, so they never overflow.
+int scale_factor(spz_state_t h, double f_re, double f_im) {
+  const double r = h->factor_re * f_re - h->factor_im * f_im;
+  const double i = h->factor_re * f_im + h->factor_im * f_re;
+  int e = 0;
+  const double mag = std::max(std::fabs(r), std::fabs(i));
+  if (mag == 0.0) return fail(SPZ_ERR_INVALID_ARGUMENT, "zero lazy factor");
+  std::frexp(mag, &e);
+  h->factor_re = std::ldexp(r, -e);
+  h->factor_im = std::ldexp(i, -e);
+  h->factor_exp += e;
+  if (h->factor_exp < -400 || h->factor_exp > 400) return settle(h);
+  return SPZ_OK;
+}
+
 int norm_sqr_to_device(spz_state_t h, double* d_out);  // reduce.cu
 
 }  // namespace spz
@@ -156,8 +234,8 @@ int spz_state_create(uint32_t n, spz_state_t* out) {
   int rc = alloc_handle(n, out);
   if (rc) return rc;
   spz_state_t h = *out;
-  cudaError_t e = cudaMalloc(&h->re, h->N * sizeof(double));
-  if (e == cudaSuccess) e = cudaMalloc(&h->im, h->N * sizeof(double));
+  cudaError_t e = dev_alloc(&h->re, h->N * sizeof(double));
+  if (e == cudaSuccess) e = dev_alloc(&h->im, h->N * sizeof(double));
   if (e != cudaSuccess) {
     if (h->re) cudaFree(h->re);
     cudaStreamDestroy(h->own_stream);
@@ -229,6 +307,8 @@ int spz_state_num_qubits(spz_state_t h, uint32_t* n) {
 
 int spz_state_device_arrays(spz_state_t h, double** d_reals, double** d_imags) {
   if (!h || !d_reals || !d_imags) return fail(SPZ_ERR_NULL, "NULL argument");
+  int rc = settle(h);  // the caller reads the arrays directly
+  if (rc) return rc;
   *d_reals = h->re;
   *d_imags = h->im;
   return SPZ_OK;
@@ -236,6 +316,7 @@ int spz_state_device_arrays(spz_state_t h, double** d_reals, double** d_imags) {
 
 int spz_state_upload(spz_state_t h, const double* reals, const double* imags) {
   if (!h || !reals || !imags) return fail(SPZ_ERR_NULL, "NULL argument");
+  clear_factor(h);
   SPZ_CUDA(cudaMemcpyAsync(h->re, reals, h->N * sizeof(double), cudaMemcpyDefault, h->stream));
   SPZ_CUDA(cudaMemcpyAsync(h->im, imags, h->N * sizeof(double), cudaMemcpyDefault, h->stream));
   SPZ_CUDA(cudaStreamSynchronize(h->stream));
@@ -244,6 +325,8 @@ int spz_state_upload(spz_state_t h, const double* reals, const double* imags) {
 
 int spz_state_download(spz_state_t h, double* reals, double* imags) {
   if (!h || !reals || !imags) return fail(SPZ_ERR_NULL, "NULL argument");
+  int rc = settle(h);
+  if (rc) return rc;
   SPZ_CUDA(cudaMemcpyAsync(reals, h->re, h->N * sizeof(double), cudaMemcpyDefault, h->stream));
   SPZ_CUDA(cudaMemcpyAsync(imags, h->im, h->N * sizeof(double), cudaMemcpyDefault, h->stream));
   SPZ_CUDA(cudaStreamSynchronize(h->stream));
@@ -252,6 +335,7 @@ int spz_state_download(spz_state_t h, double* reals, double* imags) {
 
 int spz_state_reset_zero(spz_state_t h) {
   if (!h) return fail(SPZ_ERR_NULL, "handle is NULL");
+  clear_factor(h);
   zero_state_kernel<<<grid_for(h->N), kThreads, 0, h->stream>>>(h->re, h->im, h->N);
   SPZ_CHECK_LAUNCH("zero_state_kernel");
   return SPZ_OK;
@@ -261,6 +345,9 @@ int spz_state_copy(spz_state_t dst, spz_state_t src) {
   if (!dst || !src) return fail(SPZ_ERR_NULL, "handle is NULL");
   if (dst->n != src->n) return fail(SPZ_ERR_INVALID_ARGUMENT, "qubit counts differ");
   if (dst == src) return SPZ_OK;
+  int rc = settle(src);
+  if (rc) return rc;
+  clear_factor(dst);
   // Order after src's pending work, then run on dst's stream.
   cudaEvent_t ev;
   SPZ_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
@@ -275,6 +362,7 @@ int spz_state_copy(spz_state_t dst, spz_state_t src) {
 int spz_state_fill_random(spz_state_t h, uint64_t seed, int dist, int normalise) {
   if (!h) return fail(SPZ_ERR_NULL, "handle is NULL");
   if (dist != 0 && dist != 1) return fail(SPZ_ERR_INVALID_ARGUMENT, "dist must be 0 or 1");
+  clear_factor(h);
   const uint64_t key = mix64(seed + kGolden);
   fill_kernel<<<grid_for(h->N), kThreads, 0, h->stream>>>(h->re, h->im, h->N, key, dist);
   SPZ_CHECK_LAUNCH("fill_kernel");
@@ -291,6 +379,17 @@ int spz_state_fill_random(spz_state_t h, uint64_t seed, int dist, int normalise)
     SPZ_CHECK_LAUNCH("scale_kernel");
   }
   return SPZ_OK;
+}
+
+int spz_state_set_lazy(spz_state_t h, int enable) {
+  if (!h) return fail(SPZ_ERR_NULL, "handle is NULL");
+  h->lazy = enable != 0;
+  return h->lazy ? SPZ_OK : settle(h);
+}
+
+int spz_state_settle(spz_state_t h) {
+  if (!h) return fail(SPZ_ERR_NULL, "handle is NULL");
+  return settle(h);
 }
 
 }  // extern "C"

@@ -52,8 +52,8 @@ int apply_unitary(spz_state_t h, const double* u_re, const double* u_im, uint32_
   if (control >= 0 && ((uint32_t)control >= h->n || ((uint32_t)control >= t && (uint32_t)control < t + m)))
     return fail(SPZ_ERR_INVALID_ARGUMENT, "control must be a qubit outside the unitary's block");
   if (!h->aux_re[0]) {
-    SPZ_CUDA(cudaMalloc(&h->aux_re[0], h->N * sizeof(double)));
-    cudaError_t e = cudaMalloc(&h->aux_im[0], h->N * sizeof(double));
+    SPZ_CUDA(dev_alloc(&h->aux_re[0], h->N * sizeof(double)));
+    cudaError_t e = dev_alloc(&h->aux_im[0], h->N * sizeof(double));
     if (e != cudaSuccess) {
       cudaFree(h->aux_re[0]);
       h->aux_re[0] = nullptr;

@@ -79,10 +79,18 @@ class PyQuantumTransformation:
 
 
 class QuantumCircuit:
-    """lib.rs:177-375."""
+    """lib.rs:177-375.
+
+    Takes registers as positional arguments (lib.rs:185-197).  A list of
+    registers is also accepted and unpacked: the reference's own examples pass
+    one (``QuantumCircuit([q])``, spynoza/examples/circuits.py), which its
+    constructor would reject."""
 
     def __init__(self, *registers: QuantumRegister, seed: int = 0, fused: bool = True):
-        self.qc = _c.QuantumCircuit(*registers, seed=seed, fused=fused)
+        regs: List[QuantumRegister] = []
+        for r in registers:
+            regs.extend(r if isinstance(r, (list, tuple)) else [r])
+        self.qc = _c.QuantumCircuit(*regs, seed=seed, fused=fused)
 
     @property
     def num_qubits(self) -> int:

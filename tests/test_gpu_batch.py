@@ -38,19 +38,69 @@ def test_batch_matches_single_instance_adjoint(gpu, tile_qubits, threads):
         assert info["resident_instances"] < len(insts) and info["workspace_bytes"] > 0
 
 
-@pytest.mark.parametrize("wide", [8, 1])
-def test_batch_wide_instances_run_across_the_gpu(gpu, wide):
-    """Instances of at least `wide` qubits take the whole-GPU path (fused
-    executor + fused adjoint sweep, results written on the device); the others
-    stay in the persistent kernel; replays with new angles stay right."""
+@pytest.mark.parametrize("wide,tpi", [(8, 0), (8, 1), (7, 3), (1, 2)])
+def test_batch_wide_instances_as_work_items_in_one_launch(gpu, wide, tpi):
+    """Instances of at least `wide` qubits (and more than the tile's) are
+    spread over CTAs as (pass, tile range) work items inside the persistent
+    kernel, ordered by completion counters; the rest run one per CTA; replays
+    with new angles stay right."""
     insts = _instances()
-    b = batch.Batch(insts, tile_qubits=6, threads=128, wide_qubits=wide)
+    b = batch.Batch(insts, tile_qubits=6, threads=128, wide_qubits=wide, tiles_per_item=tpi)
+    info = b.info()
+    assert info["wide_in_kernel"] == sum(1 for i in insts if i[0] >= max(wide, 7)) and info["wide_separate"] == 0
+    assert info["work_items"] > len(insts) - info["wide_in_kernel"]
     for shift in (0.0, 0.21):
         theta = b.theta + shift
         e, g = b.run(theta)
         for i, (n, ops, pidx, _, terms) in enumerate(insts):
             th = b.split(theta)[i]
             e1, g1 = adjoint.adjoint_gradient(State(n), adjoint.set_params(ops, pidx, th), pidx, terms)
+            assert abs(e[i] - e1) < 1e-12 * max(1.0, abs(e1)), (i, e[i], e1)
+            np.testing.assert_allclose(b.split(g)[i], g1, atol=1e-11, rtol=0)
+    e2, g2 = b.run(b.theta + 0.21)  # deterministic: fixed items, slots and fold order
+    assert np.array_equal(e2, e) and np.array_equal(g2, g)
+
+
+def test_batch_wide_item_wait_times_out_cleanly(gpu):
+    """A dependency wait that never completes (a host-side injection makes the
+    wide items of later passes wait for a count no item reaches) ends the
+    launch with SPZ_ERR_TIMEOUT instead of hanging; the context stays usable."""
+    import os
+
+    from spinoza_gb300 import _native as nat
+
+    insts = _instances()
+    os.environ["SPZ_BATCH_TEST_STALL"] = "1"
+    try:
+        b = batch.Batch(insts, tile_qubits=6, threads=128, wide_qubits=8)
+    finally:
+        os.environ.pop("SPZ_BATCH_TEST_STALL", None)
+    with pytest.raises(nat.SpzError) as info:
+        b.run()
+    assert info.value.code == nat.SPZ_ERR_TIMEOUT
+    b.close()
+    ok = batch.Batch(insts, tile_qubits=6, threads=128, wide_qubits=8)
+    e, g = ok.run()
+    e1, g1 = _single(insts[4])
+    assert abs(e[4] - e1) < 1e-12 * max(1.0, abs(e1))
+    np.testing.assert_allclose(ok.split(g)[4], g1, atol=1e-11, rtol=0)
+
+
+@pytest.mark.parametrize("wide", [8, 1])
+def test_batch_wide_instances_fast_run_across_the_gpu(gpu, wide):
+    """With the fast adjoint, instances of at least `wide` qubits take the
+    whole-GPU path (fused executor + fused fast adjoint sweep, results written
+    on the device); the others stay in the persistent kernel."""
+    insts = _instances()
+    b = batch.Batch(insts, tile_qubits=6, threads=128, wide_qubits=wide, fast=True)
+    assert b.info()["wide_separate"] == sum(1 for i in insts if i[0] >= max(wide, 7))
+    for shift in (0.0, 0.21):
+        theta = b.theta + shift
+        e, g = b.run(theta)
+        for i, (n, ops, pidx, _, terms) in enumerate(insts):
+            th = b.split(theta)[i]
+            e1, g1 = adjoint.adjoint_gradient(State(n), adjoint.set_params(ops, pidx, th), pidx, terms,
+                                              fast=n >= max(wide, 7))
             assert abs(e[i] - e1) < 1e-12 * max(1.0, abs(e1)), (i, e[i], e1)
             np.testing.assert_allclose(b.split(g)[i], g1, atol=1e-11, rtol=0)
 
@@ -102,3 +152,19 @@ def test_config5_generator_shapes():
     for n, ops, pidx, theta, terms in insts:
         assert len(pidx) % (2 * n) == 0 and 2 <= len(pidx) // (2 * n) <= 10
         assert len(terms) == 2 * n - 1
+
+
+def test_autotuner_times_candidates_and_caches(gpu, tmp_path, monkeypatch):
+    monkeypatch.setenv("SPZ_AUTOTUNE_CACHE", str(tmp_path))
+    insts = _instances()
+    cands = [(6, 64, 1), (6, 128, 4)]
+    best = batch.autotune(insts, candidates=cands, sample=8)
+    assert (best["tile_qubits"], best["threads"], best["tiles_per_item"]) in cands
+    assert len(best["candidates"]) == 2 and best["sample"] <= len(insts)
+    again = batch.autotune(insts, candidates=[(5, 64, 2)])  # answered from the cache
+    assert again == best
+    b = batch.Batch(insts, tile_qubits=best["tile_qubits"], threads=best["threads"],
+                    tiles_per_item=best["tiles_per_item"])
+    e, g = b.run()
+    e1, g1 = _single(insts[5])
+    assert abs(e[5] - e1) < 1e-12 * max(1.0, abs(e1))

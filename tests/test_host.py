@@ -267,3 +267,29 @@ def test_reference_arm_does_not_load_the_product_library():
     assert line["impl"] == "reference" and line["value"] > 0
     assert line["config"] == __import__("bench").workload_config(12, 4)
     assert probe == {"pkg": [], "so": False}
+
+
+def test_ctypes_struct_sizes_match_the_c_header(tmp_path):
+    """Compile the header with gcc and compare sizeof of every struct with the
+    ctypes mirrors the Python layer passes across the ABI."""
+    import ctypes
+    import shutil
+    import subprocess
+
+    gcc = shutil.which("gcc")
+    if not gcc:
+        pytest.skip("gcc not available")
+    names = {"spz_gate": nat.spz_gate, "spz_op": nat.spz_op, "spz_tracker": nat.spz_tracker,
+             "spz_exec_stats": nat.spz_exec_stats, "spz_pauli_term": nat.spz_pauli_term,
+             "spz_batch_instance": nat.spz_batch_instance, "spz_batch_config": nat.spz_batch_config,
+             "spz_batch_stats": nat.spz_batch_stats}
+    src = tmp_path / "sizes.c"
+    src.write_text('#include <stdio.h>\n#include "spinoza_gb300.h"\nint main(void) {\n' +
+                   "".join(f'  printf("{k} %zu\\n", sizeof({k}));\n' for k in names) + "  return 0;\n}\n")
+    exe = tmp_path / "sizes"
+    subprocess.run([gcc, "-I", str(HEADER.parent), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout
+    got = {ln.split()[0]: int(ln.split()[1]) for ln in out.splitlines()}
+    for k, ct in names.items():
+        assert got[k] == ctypes.sizeof(ct), k
+    assert nat.INSTANCE_DTYPE.itemsize == got["spz_batch_instance"]
