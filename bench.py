@@ -389,6 +389,7 @@ def gpu_arm(args) -> None:
     abytes = algorithmic_bytes(ops, n)
     N = 1 << n
     mode = nat.EXEC_DEFAULT if args.exact else nat.EXEC_FAST
+    mode |= {"threads": 0, "tma": nat.EXEC_TMA, "tma-prefetch": nat.EXEC_TMA_PREFETCH}[args.staging]
     re_t = torch.empty(N, dtype=torch.float64, device="cuda")
     im_t = torch.empty(N, dtype=torch.float64, device="cuda")
     state = State.from_torch(re_t, im_t)
@@ -538,6 +539,7 @@ def gpu_arm(args) -> None:
             "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": workload_config(n, layers),
+            "staging": args.staging,
             "executor": ("fused shared-memory tile passes, exact reference arithmetic" if args.exact else
                          "fused shared-memory tile passes, fast arithmetic (lazy scaling, U = P RY P, phases pushed "
                          "through permutations); equal to exact up to rounding"),
@@ -696,7 +698,8 @@ def batch_bench(args) -> dict:
             else {"tile_qubits": args.batch_tile, "threads": args.batch_threads, "tiles_per_item": args.batch_tpi})
     t0 = time.perf_counter()
     b = batch.Batch(insts, tile_qubits=tune["tile_qubits"], threads=tune["threads"], wide_qubits=args.batch_wide,
-                    fast=args.batch_fast, tiles_per_item=tune.get("tiles_per_item", 0))
+                    fast=args.batch_fast, tiles_per_item=tune.get("tiles_per_item", 0),
+                    wide_apart=args.batch_apart)
     t_plan = time.perf_counter() - t0
     b.run()
     steps = max(1, args.batch_steps)
@@ -742,6 +745,8 @@ def batch_bench(args) -> dict:
                         f"depth U{{2..10}}, seeds 8+k", "instances": len(insts), "params": nparams,
             "qubits_min": min(qs), "qubits_max": max(qs), "launch": tune,
             "wide_qubits": args.batch_wide or 18, "wide_adjoint": "fast" if args.batch_fast else "exact",
+            "wide_path": ("one at a time across the GPU" if args.batch_fast or args.batch_apart else
+                          "work items inside the persistent launch"),
             "seconds_per_batch": t_batch, "instances_per_s": len(insts) / t_batch, "grads_per_s": nparams / t_batch,
             "loop_seconds_extrapolated": t_loop, "loop_sample": len(sample), "speedup_vs_loop": t_loop / t_batch,
             "max_abs_energy_diff_vs_loop": max_e, "max_abs_grad_diff_vs_loop": max_g,
@@ -758,6 +763,33 @@ def workload_batch(args) -> None:
     _line("config5 batched forward+adjoint instances/s", d["instances_per_s"], "instances/s", args,
           higher_is_better=True, config={"workload": d["workload"], "params": d["params"], "launch": d["launch"]},
           batch=d)
+
+
+def workload_gate(args) -> None:
+    """One gate kind on one target through spz_apply, exact or lazy, repeated:
+    the case the per-gate kernels' profiles are taken on."""
+    import torch
+
+    from spinoza_gb300 import gates
+    from spinoza_gb300.core import State
+    from spinoza_gb300.gates import Gate
+
+    n = args.qubits
+    N = 1 << n
+    s = State(n)
+    s.fill_random(11, "uniform", normalise=True)
+    s.set_stream(torch.cuda.current_stream())
+    s.set_lazy(args.lazy)
+    g = {"H": Gate.H, "X": Gate.X, "RX": Gate.RX(0.7), "RY": Gate.RY(0.7), "RZ": Gate.RZ(0.7),
+         "U": Gate.U(0.3, 0.4, 0.5)}[args.gate]
+    dt = _event_time(lambda: gates.apply(g, s, args.target), args.steps, args.warmup)
+    s.settle()
+    peaks = measured_peaks()
+    gbs = 32 * N / dt / 1e9
+    _line(f"{args.gate} gate at {n} qubits ({'lazy' if args.lazy else 'exact'})", gbs, "GB/s", args,
+          higher_is_better=True, config={"workload": f"{args.gate} on target {args.target}, {n} qubits",
+                                         "mode": "lazy" if args.lazy else "exact"},
+          ms=dt * 1e3, hbm_frac=gbs / peaks["hbm_gbs"], peak_gbs=peaks["hbm_gbs"])
 
 
 def workload_sweep33(args) -> None:
@@ -804,7 +836,11 @@ def main() -> None:
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="brickwork", choices=["brickwork", "qft20", "measure28", "batch", "sweep33"])
+    ap.add_argument("--workload", default="brickwork",
+                    choices=["brickwork", "qft20", "measure28", "batch", "sweep33", "gate"])
+    ap.add_argument("--gate", default="H", choices=["H", "X", "RX", "RY", "RZ", "U"], help="gate workload: kind")
+    ap.add_argument("--target", type=int, default=5, help="gate workload: target qubit")
+    ap.add_argument("--lazy", action="store_true", help="gate workload: the lazy per-gate mode")
     ap.add_argument("--qubits", type=int, default=30)
     ap.add_argument("--layers", type=int, default=20)
     ap.add_argument("--instances", type=int, default=4096)
@@ -813,6 +849,7 @@ def main() -> None:
     ap.add_argument("--no-batch", action="store_true", help="headline line without the config-5 batch object")
     ap.add_argument("--batch-steps", type=int, default=1, help="timed runs of the config-5 batch")
     ap.add_argument("--batch-tpi", type=int, default=0, help="batch workload: tiles per work item of a wide instance")
+    ap.add_argument("--batch-apart", action="store_true", help="batch workload: wide instances one at a time")
     ap.add_argument("--batch-tile", type=int, default=11, help="batch workload: tile qubits (resident up to this n)")
     ap.add_argument("--batch-threads", type=int, default=128, help="batch workload: threads per block")
     ap.add_argument("--batch-qmax", type=int, default=22, help="batch workload: largest instance (small profiling cases)")
@@ -826,6 +863,8 @@ def main() -> None:
     ap.add_argument("--no-parity", action="store_true")
     ap.add_argument("--no-sweep", action="store_true", help="skip the per-gate sweep at the headline's qubit count")
     ap.add_argument("--exact", action="store_true", help="time the bit-exact executor mode instead of fast mode")
+    ap.add_argument("--staging", default="threads", choices=["threads", "tma", "tma-prefetch"],
+                    help="how fused passes load their tiles: thread loads (default) or TMA gathers")
     args = ap.parse_args()
     if args.impl == "reference":
         reference_arm(args)
@@ -836,7 +875,7 @@ def main() -> None:
 
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         {"qft20": workload_qft20, "measure28": workload_measure28, "batch": workload_batch,
-         "sweep33": workload_sweep33}[args.workload](args)
+         "sweep33": workload_sweep33, "gate": workload_gate}[args.workload](args)
 
 
 if __name__ == "__main__":

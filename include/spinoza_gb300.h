@@ -212,6 +212,11 @@ typedef struct spz_tracker {
 #define SPZ_EXEC_FAST 8u         /* fused, with arithmetic rewritten to need fewer FP64
                                     instructions (lazy scaling, phase pushing); equal to
                                     the exact mode up to rounding, not bit-identical     */
+#define SPZ_EXEC_TMA 32u         /* fused tile passes load each tile with the Tensor
+                                    Memory Accelerator (gathers of four 64-byte rows)
+                                    instead of thread loads; same results               */
+#define SPZ_EXEC_TMA_PREFETCH 64u /* as SPZ_EXEC_TMA, and the next tile is fetched while
+                                    the current one computes (two tile buffers)          */
 
 /* Execution counters filled by spz_circuit_execute (may be NULL). */
 typedef struct spz_exec_stats {
@@ -386,9 +391,14 @@ typedef struct spz_batch_config {
                              of them under SPZ_EXEC_FAST, run one at a time across
                              the GPU instead (fused executor + fused adjoint sweep) */
   int32_t flags;          /* SPZ_EXEC_FAST: the wide instances use the fast adjoint
-                             (equal to the exact one up to rounding)                 */
+                             (equal to the exact one up to rounding), one at a time
+                             across the GPU; SPZ_BATCH_WIDE_APART: the wide instances
+                             run one at a time across the GPU in the exact mode too
+                             (no per-instance workspace held for the whole run)      */
   int32_t tiles_per_item; /* tiles per work item of a wide instance (0 = 16)       */
 } spz_batch_config;
+
+#define SPZ_BATCH_WIDE_APART 16
 
 typedef struct spz_batch_stats {
   uint64_t instances, resident_instances;

@@ -36,6 +36,9 @@ EXEC_DEFAULT = 0
 EXEC_UNFUSED = 1
 EXEC_TIME_PASSES = 4
 EXEC_FAST = 8
+BATCH_WIDE_APART = 16
+EXEC_TMA = 32
+EXEC_TMA_PREFETCH = 64
 MAX_QUBITS = 34
 
 

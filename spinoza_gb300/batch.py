@@ -69,15 +69,17 @@ class Batch:
     """A planned, device-resident batch; run(theta) -> (energies, grads)."""
 
     def __init__(self, instances: Sequence[Instance], tile_qubits: int = 0, threads: int = 0, wide_qubits: int = 0,
-                 fast: bool = False, tiles_per_item: int = 0):
+                 fast: bool = False, tiles_per_item: int = 0, wide_apart: bool = False):
         """tile_qubits / threads: launch shape of the persistent kernel;
         wide_qubits: instances of at least this many qubits are spread over
         many CTAs as work items of tiles_per_item tiles (0: the library's
         defaults, 31: never); fast: those run one at a time across the GPU with
-        the fast adjoint (equal to the exact one up to rounding)."""
+        the fast adjoint (equal to the exact one up to rounding); wide_apart:
+        they run one at a time across the GPU in the exact mode."""
         self.inst, self.ops, self.pidx, self.theta, self.terms = pack(instances)
         cfg = nat.spz_batch_config(int(tile_qubits), int(threads), int(wide_qubits),
-                                   nat.EXEC_FAST if fast else nat.EXEC_DEFAULT, int(tiles_per_item))
+                                   (nat.EXEC_FAST if fast else nat.EXEC_DEFAULT) |
+                                   (nat.BATCH_WIDE_APART if wide_apart else 0), int(tiles_per_item))
         h = c_void_p()
         nat.check(nat.lib().spz_batch_create(nat.ptr(self.inst), len(self.inst), nat.ptr(self.ops),
                                              nat.ptr(self.pidx), nat.ptr(self.terms), byref(cfg), byref(h)))

@@ -47,7 +47,9 @@ namespace {
 
 constexpr int kBatchMaxK = 12;
 constexpr int kBatchLowBits = 3;
-constexpr int kMaxPassParams = 256;  // gradient accumulators per backward pass
+// Gradient accumulators per backward pass (passes with more parameters are
+// split); each warp keeps its own set in shared memory.
+constexpr int kMaxPassParams = 64;
 constexpr uint64_t kWorkspaceBudget = 128ull << 30;  // HBM for streamed instances' psi and lam
 // From about 2^18 amplitudes one instance (with two more running beside it on
 // other streams) keeps the GPU's block slots busy; below, one CTA per instance
@@ -286,8 +288,9 @@ __device__ void run_pass(const BatchArgs& A, const BInst& I, const BPass& P, uin
       rowoff[r] = off;
     }
   }
+  const int nwarps = (int)(blockDim.x >> 5), warp = (int)(threadIdx.x >> 5), lane = (int)(threadIdx.x & 31);
   if (P.kind == BP_BWD)
-    for (int j = threadIdx.x; j < P.nparams; j += blockDim.x) S.gacc[j] = 0.0;
+    for (int j = threadIdx.x; j < nwarps * kMaxPassParams; j += blockDim.x) S.gacc[j] = 0.0;
   __syncthreads();
   for (uint64_t tile = t0; tile < t1; ++tile) {
     const uint64_t base = I.resident ? 0 : deposit(tile, P.lpos, K);
@@ -356,8 +359,11 @@ __device__ void run_pass(const BatchArgs& A, const BInst& I, const BPass& P, uin
         const BGate& g = A.gates[P.gate_begin + gi];
         if ((base & g.g_ones) != g.g_ones || (base & g.g_zeros) != 0) continue;
         if (g.grad != BG_NONE) {
-          const double part = bsum(b_grad_part(g, base, pr, pi, lr, li, T), S.red);
-          if (threadIdx.x == 0) S.gacc[g.gacc] = dadd(S.gacc[g.gacc], part);
+          // this warp's share, into its own accumulator (no block reduction per tile)
+          double part = b_grad_part(g, base, pr, pi, lr, li, T);
+          for (int off = 16; off > 0; off >>= 1) part = dadd(part, __shfl_down_sync(0xffffffffu, part, off));
+          if (lane == 0) S.gacc[warp * kMaxPassParams + g.gacc] = dadd(S.gacc[warp * kMaxPassParams + g.gacc], part);
+          __syncthreads();  // every read of psi and lam for the gradient precedes the update
         }
         b_apply(g, base, pr, pi, T);
         b_apply(g, base, lr, li, T);
@@ -381,6 +387,14 @@ __device__ void run_pass(const BatchArgs& A, const BInst& I, const BPass& P, uin
           *reinterpret_cast<double2*>(wli + gi) = *reinterpret_cast<const double2*>(li + e);
         }
       }
+    }
+    __syncthreads();
+  }
+  if (P.kind == BP_BWD) {  // the warps' accumulators, summed in warp order, into row 0
+    for (int j = threadIdx.x; j < P.nparams; j += blockDim.x) {
+      double v = S.gacc[j];
+      for (int w = 1; w < nwarps; ++w) v = dadd(v, S.gacc[w * kMaxPassParams + j]);
+      S.gacc[j] = v;
     }
     __syncthreads();
   }
@@ -724,7 +738,8 @@ int build_batch(spz_batch_t b, const spz_batch_instance* inst, size_t ninst, con
     // (SPZ_EXEC_FAST) and anything beyond the budget take the whole-GPU path.
     const bool wide = (int)n >= b->wide_qubits && (int)n > b->kmax;
     const uint64_t ws_need = 4ull * (1ull << n);
-    const bool in_kernel = wide && !(b->wide_flags & SPZ_EXEC_FAST) && (wide_ws + ws_need) * 8 <= wide_budget;
+    const bool in_kernel = wide && !(b->wide_flags & (SPZ_EXEC_FAST | SPZ_BATCH_WIDE_APART)) &&
+                           (wide_ws + ws_need) * 8 <= wide_budget;
     if (wide && in_kernel) {
       wide_index[ii] = (int32_t)wide_in.size();
       wide_in.push_back((uint32_t)ii);
@@ -1056,7 +1071,7 @@ int build_batch(spz_batch_t b, const spz_batch_instance* inst, size_t ninst, con
   SPZ_CUDA(host_alloc(&b->h_energy, std::max<size_t>(1, ninst) * sizeof(double)));
   // launch shape: persistent CTAs, as many per SM as shared memory allows
   const uint32_t TMAX = 1u << b->kmax;
-  b->smem = (4 * TMAX + (TMAX >> kBatchLowBits) + 64 + kMaxPassParams) * sizeof(double);
+  b->smem = (4 * TMAX + (TMAX >> kBatchLowBits) + 64 + (size_t)(b->threads / 32) * kMaxPassParams) * sizeof(double);
   SPZ_CUDA(cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem));
   int per_sm = 0;
   SPZ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel, b->threads, b->smem));
@@ -1136,7 +1151,7 @@ int spz_batch_create(const spz_batch_instance* instances, size_t ninstances, con
     if (config->tile_qubits) b->kmax = config->tile_qubits;
     if (config->threads) b->threads = config->threads;
     if (config->wide_qubits) b->wide_qubits = config->wide_qubits;
-    b->wide_flags = (uint32_t)config->flags & SPZ_EXEC_FAST;
+    b->wide_flags = (uint32_t)config->flags & (SPZ_EXEC_FAST | SPZ_BATCH_WIDE_APART);
     if (config->tiles_per_item) b->tiles_per_item = config->tiles_per_item;
   }
   {  // host-side fault injection for tests: wide items wait on counts never reached
@@ -1205,7 +1220,7 @@ int spz_batch_run(spz_batch_t b, const double* theta, double* energies, double* 
     int rc = spz_state_reset_zero(h);
     if (!rc)
       rc = adjoint_gradient(h, w.ops.data(), w.ops.size(), w.pidx.data(), w.pidx.size(), w.terms.data(),
-                            w.terms.size(), b->wide_flags, nullptr, nullptr, b->d_energy + w.idx,
+                            w.terms.size(), b->wide_flags & SPZ_EXEC_FAST, nullptr, nullptr, b->d_energy + w.idx,
                             b->d_grad + w.param_offset);
     if (rc) {
       wait_all();

@@ -14,6 +14,9 @@
 // reference's own operations).  The planner keeps program order except where a
 // swap of two gates is bit-exact (see ExactClass below).  So a fused run is
 // bit-identical to the sequential one.
+#include <cuda.h>  // CUtensorMap (the encoder is reached through the runtime's driver entry point)
+#include <cudaTypedefs.h>
+
 #include <algorithm>
 #include <cstring>
 #include <vector>
@@ -187,6 +190,62 @@ __device__ __forceinline__ void tile_phase_pm(const TileGate& g, const double2* 
   }
 }
 
+// Every gate of the pass on one tile held in shared memory (sre, sim), in
+// pass order, with a block barrier after each.
+__device__ __forceinline__ void tile_pass_gates(const PassArgs& A, uint64_t base, double* sre, double* sim,
+                                                uint32_t T) {
+  for (int gi = 0; gi < A.ngates; ++gi) {
+    const TileGate& g = A.gates[gi];
+    if ((base & g.g_ones) != g.g_ones || (base & g.g_zeros) != 0) continue;  // uniform per tile
+    if (g.cond >= 0 && A.outcomes[g.cond] == 0) continue;                   // classical condition
+    const uint32_t nw = T >> g.npos;
+    switch (g.mode) {
+      case TM_PAIR:
+        switch (g.kind) {
+          case SPZ_GATE_H: tile_pair_any<SPZ_GATE_H, TileGate, TileSwizzle>(g, sre, sim, nw); break;
+          case SPZ_GATE_X: tile_pair_any<SPZ_GATE_X, TileGate, TileSwizzle>(g, sre, sim, nw); break;
+          case SPZ_GATE_Y: tile_pair_any<SPZ_GATE_Y, TileGate, TileSwizzle>(g, sre, sim, nw); break;
+          case SPZ_GATE_RX: tile_pair_any<SPZ_GATE_RX, TileGate, TileSwizzle>(g, sre, sim, nw); break;
+          case SPZ_GATE_RY: tile_pair_any<SPZ_GATE_RY, TileGate, TileSwizzle>(g, sre, sim, nw); break;
+#define SPZ_LAZY(FK)                                                            \
+  case FK:                                                                      \
+    if (g.pm) tile_fast_phase_pm<FK>(g, A.tables + g.ptab, base, sre, sim, nw); \
+    else tile_pair<FK, 1, TileGate, TileSwizzle>(g, sre, sim, nw);              \
+    break;
+          SPZ_LAZY(FK_LAZY_H)
+          SPZ_LAZY(FK_LAZY_RX_A)
+          SPZ_LAZY(FK_LAZY_RX_B)
+          SPZ_LAZY(FK_LAZY_RY_A)
+          SPZ_LAZY(FK_LAZY_RY_B)
+#undef SPZ_LAZY
+          default: tile_pair_any<SPZ_GATE_U, TileGate, TileSwizzle>(g, sre, sim, nw); break;
+        }
+        break;
+      case TM_PHASE:
+        if (g.npos) tile_phase_pm<1>(g, A.tables + g.ptab, base, sre, sim, nw);
+        else tile_phase_pm<0>(g, A.tables + g.ptab, base, sre, sim, nw);
+        break;
+      case TM_DIAG_LOCAL:
+      case TM_DIAG_GLOBAL: {
+        int gone = -1;
+        if (g.mode == TM_DIAG_GLOBAL) {
+          gone = (base & g.g_tbit) ? 1 : 0;
+          if (!gone && g.kind != SPZ_GATE_RZ) break;  // Z / P act on the 1 half only
+        }
+        switch (g.kind) {
+          case SPZ_GATE_Z: tile_diag_any<SPZ_GATE_Z, TileGate, TileSwizzle>(g, sre, sim, nw, gone); break;
+          case SPZ_GATE_P: tile_diag_any<SPZ_GATE_P, TileGate, TileSwizzle>(g, sre, sim, nw, gone); break;
+          default: tile_diag_any<SPZ_GATE_RZ, TileGate, TileSwizzle>(g, sre, sim, nw, gone); break;
+        }
+        break;
+      }
+      default:  // TM_SWAP
+        tile_swap_any<TileGate, TileSwizzle>(g, sre, sim, nw);
+    }
+    __syncthreads();
+  }
+}
+
 __global__ void __launch_bounds__(kTileThreads, SPZ_TILE_MIN_BLOCKS) tile_kernel(PassArgs A) {
   extern __shared__ double smem[];
   const int K = A.k;
@@ -228,56 +287,7 @@ __global__ void __launch_bounds__(kTileThreads, SPZ_TILE_MIN_BLOCKS) tile_kernel
       *reinterpret_cast<double2*>(sim + p) = m;
     }
     __syncthreads();
-    for (int gi = 0; gi < A.ngates; ++gi) {
-      const TileGate& g = A.gates[gi];
-      if ((base & g.g_ones) != g.g_ones || (base & g.g_zeros) != 0) continue;  // uniform per tile
-      if (g.cond >= 0 && A.outcomes[g.cond] == 0) continue;                   // classical condition
-      const uint32_t nw = T >> g.npos;
-      switch (g.mode) {
-        case TM_PAIR:
-          switch (g.kind) {
-            case SPZ_GATE_H: tile_pair_any<SPZ_GATE_H, TileGate, TileSwizzle>(g, sre, sim, nw); break;
-            case SPZ_GATE_X: tile_pair_any<SPZ_GATE_X, TileGate, TileSwizzle>(g, sre, sim, nw); break;
-            case SPZ_GATE_Y: tile_pair_any<SPZ_GATE_Y, TileGate, TileSwizzle>(g, sre, sim, nw); break;
-            case SPZ_GATE_RX: tile_pair_any<SPZ_GATE_RX, TileGate, TileSwizzle>(g, sre, sim, nw); break;
-            case SPZ_GATE_RY: tile_pair_any<SPZ_GATE_RY, TileGate, TileSwizzle>(g, sre, sim, nw); break;
-#define SPZ_LAZY(FK)                                                          \
-  case FK:                                                                    \
-    if (g.pm) tile_fast_phase_pm<FK>(g, A.tables + g.ptab, base, sre, sim, nw); \
-    else tile_pair<FK, 1, TileGate, TileSwizzle>(g, sre, sim, nw);            \
-    break;
-            SPZ_LAZY(FK_LAZY_H)
-            SPZ_LAZY(FK_LAZY_RX_A)
-            SPZ_LAZY(FK_LAZY_RX_B)
-            SPZ_LAZY(FK_LAZY_RY_A)
-            SPZ_LAZY(FK_LAZY_RY_B)
-#undef SPZ_LAZY
-            default: tile_pair_any<SPZ_GATE_U, TileGate, TileSwizzle>(g, sre, sim, nw); break;
-          }
-          break;
-        case TM_PHASE:
-          if (g.npos) tile_phase_pm<1>(g, A.tables + g.ptab, base, sre, sim, nw);
-          else tile_phase_pm<0>(g, A.tables + g.ptab, base, sre, sim, nw);
-          break;
-        case TM_DIAG_LOCAL:
-        case TM_DIAG_GLOBAL: {
-          int gone = -1;
-          if (g.mode == TM_DIAG_GLOBAL) {
-            gone = (base & g.g_tbit) ? 1 : 0;
-            if (!gone && g.kind != SPZ_GATE_RZ) break;  // Z / P act on the 1 half only
-          }
-          switch (g.kind) {
-            case SPZ_GATE_Z: tile_diag_any<SPZ_GATE_Z, TileGate, TileSwizzle>(g, sre, sim, nw, gone); break;
-            case SPZ_GATE_P: tile_diag_any<SPZ_GATE_P, TileGate, TileSwizzle>(g, sre, sim, nw, gone); break;
-            default: tile_diag_any<SPZ_GATE_RZ, TileGate, TileSwizzle>(g, sre, sim, nw, gone); break;
-          }
-          break;
-        }
-        default:  // TM_SWAP
-          tile_swap_any<TileGate, TileSwizzle>(g, sre, sim, nw);
-      }
-      __syncthreads();
-    }
+    tile_pass_gates(A, base, sre, sim, T);
     // store
     for (uint32_t e2 = threadIdx.x; e2 < T / 2; e2 += blockDim.x) {
       const uint32_t e = 2 * e2;
@@ -293,6 +303,144 @@ __global__ void __launch_bounds__(kTileThreads, SPZ_TILE_MIN_BLOCKS) tile_kernel
       *reinterpret_cast<double2*>(A.im + gi) = m;
     }
     __syncthreads();
+  }
+}
+
+
+// ------------------------------------------------------------ TMA staging
+// The same pass with each tile fetched by the Tensor Memory Accelerator: the
+// state is viewed as 2^(n-3) rows of 8 doubles (one 64-byte row per value of
+// the three low qubits, which every pass keeps local), and a tile's 2^(k-3)
+// rows, at scattered row indices, arrive by cp.async.bulk.tensor gathers of
+// four rows each (tile::gather4), issued by the first warp and counted on an
+// mbarrier.  PREFETCH keeps two tile buffers and fetches the next tile while
+// the current one computes.  Compute and store are the thread-load kernel's,
+// so the results are identical.  Waits are bounded: past the limit the block
+// records the timeout in *err, waits (bounded) for its copies in flight and
+// returns; the call then reports SPZ_ERR_TIMEOUT.
+#ifndef SPZ_TMA_WAIT_POLLS
+#define SPZ_TMA_WAIT_POLLS (1u << 24)
+#endif
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n"
+      "  .reg .pred p;\n"
+      "  mbarrier.try_wait.parity.acquire.cta.shared::cta.b64 p, [%1], %2;\n"
+      "  selp.u32 %0, 1, 0, p;\n"
+      "}\n"
+      : "=r"(done)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, uint32_t parity) {
+  for (uint32_t i = 0; i < SPZ_TMA_WAIT_POLLS; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+// Four 64-byte rows (row indices r0..r3 of the 8-column view) into 256
+// contiguous bytes of shared memory; completion counted on `bar`.
+__device__ __forceinline__ void tma_gather4(double* dst, const CUtensorMap* map, int r0, int r1, int r2, int r3,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile::gather4.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4, %5, %6}], [%7];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(0), "r"(r0), "r"(r1), "r"(r2), "r"(r3), "r"(smem_u32(bar))
+      : "memory");
+}
+
+template <bool PREFETCH>
+__global__ void __launch_bounds__(kTileThreads) tile_kernel_tma(PassArgs A, const __grid_constant__ CUtensorMap map_re,
+                                                                const __grid_constant__ CUtensorMap map_im, int* err) {
+  extern __shared__ double smem_raw[];
+  __shared__ __align__(8) uint64_t bars[2];
+  const int K = A.k;
+  const uint32_t T = 1u << K;
+  const uint32_t nrows = T >> kTileLowBits;
+  // tile buffers at a 128-byte boundary (the gathers' destinations)
+  double* bufs = reinterpret_cast<double*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~(uintptr_t)127);
+  constexpr int kBufs = PREFETCH ? 2 : 1;
+  uint64_t* rowoff = reinterpret_cast<uint64_t*>(bufs + 2 * kBufs * T);
+  for (uint32_t r = threadIdx.x; r < nrows; r += blockDim.x) {
+    uint64_t off = 0;
+    for (int j = 0; j < A.nhigh; ++j)
+      if ((r >> j) & 1) off |= 1ull << A.lpos[kTileLowBits + j];
+    rowoff[r] = off;
+  }
+  if (threadIdx.x == 0) {
+    for (int b = 0; b < kBufs; ++b) mbar_init(&bars[b], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  __syncthreads();
+  const uint32_t lane = threadIdx.x & 31u;
+  const bool issuer = threadIdx.x < 32;
+  auto issue = [&](uint64_t tile, int b) {  // the first warp; after the buffer's last generic access
+    if (!issuer) return;
+    const uint64_t base = deposit(tile, A.lpos, K);
+    if (lane == 0) mbar_arrive_expect_tx(&bars[b], 2u * T * (uint32_t)sizeof(double));
+    __syncwarp();
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    double* dre = bufs + (size_t)b * 2 * T;
+    double* dim = dre + T;
+    for (uint32_t j = lane; j < nrows / 4; j += 32) {
+      const int r0 = (int)((base | rowoff[4 * j + 0]) >> kTileLowBits);
+      const int r1 = (int)((base | rowoff[4 * j + 1]) >> kTileLowBits);
+      const int r2 = (int)((base | rowoff[4 * j + 2]) >> kTileLowBits);
+      const int r3 = (int)((base | rowoff[4 * j + 3]) >> kTileLowBits);
+      tma_gather4(dre + 32 * j, &map_re, r0, r1, r2, r3, &bars[b]);
+      tma_gather4(dim + 32 * j, &map_im, r0, r1, r2, r3, &bars[b]);
+    }
+  };
+  uint32_t parity[2] = {0u, 0u};
+  uint64_t tile = A.tile_begin + blockIdx.x;
+  if (tile < A.ntiles) issue(tile, 0);
+  int b = 0;
+  for (; tile < A.ntiles; tile += gridDim.x) {
+    const uint64_t next = tile + gridDim.x;
+    bool pending_next = false;
+    if (PREFETCH && next < A.ntiles) {
+      issue(next, b ^ 1);
+      pending_next = true;
+    }
+    const bool ok = mbar_wait_bounded(&bars[b], parity[b]);
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) {
+        atomicExch(err, 1);
+        mbar_wait_bounded(&bars[b], parity[b]);
+        if (pending_next) mbar_wait_bounded(&bars[b ^ 1], parity[b ^ 1]);
+      }
+      __syncthreads();
+      return;
+    }
+    parity[b] ^= 1u;
+    double* sre = bufs + (size_t)b * 2 * T;
+    double* sim = sre + T;
+    const uint64_t base = deposit(tile, A.lpos, K);
+    tile_pass_gates(A, base, sre, sim, T);
+    for (uint32_t e2 = threadIdx.x; e2 < T / 2; e2 += blockDim.x) {  // store, as the thread-load kernel
+      const uint32_t e = 2 * e2;
+      const uint64_t gi = base | rowoff[e >> kTileLowBits] | (e & ((1u << kTileLowBits) - 1));
+      *reinterpret_cast<double2*>(A.re + gi) = *reinterpret_cast<const double2*>(sre + e);
+      *reinterpret_cast<double2*>(A.im + gi) = *reinterpret_cast<const double2*>(sim + e);
+    }
+    __syncthreads();
+    if (!PREFETCH && next < A.ntiles) issue(next, 0);
+    if (PREFETCH) b ^= 1;
   }
 }
 
@@ -582,6 +730,63 @@ int tile_launch_shape(int device, int threads, size_t smem, int* resident_out, i
   return SPZ_OK;
 }
 
+// TMA staging: tensor maps of the handle's arrays, 2^(n-3) rows of 8 doubles
+// (64-byte rows, boxes one row high as tile::gather4 requires), built once.
+int ensure_tma_maps(spz_state_t h) {
+  if (h->tma_ready) return SPZ_OK;
+  if (h->n < 5) return fail(SPZ_ERR_UNSUPPORTED, "TMA staging needs at least 5 qubits");
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  static std::mutex mu;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    if (!encode) {
+      void* fn = nullptr;
+      cudaDriverEntryPointQueryResult q{};
+      SPZ_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q));
+      if (q != cudaDriverEntryPointSuccess || !fn) return fail(SPZ_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled unavailable");
+      encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+    }
+  }
+  double* arrays[2] = {h->re, h->im};
+  for (int a = 0; a < 2; ++a) {
+    if (reinterpret_cast<uintptr_t>(arrays[a]) & 15) return fail(SPZ_ERR_UNSUPPORTED, "TMA needs 16-byte aligned arrays");
+    alignas(64) CUtensorMap m;
+    const cuuint64_t dims[2] = {8, h->N >> 3};
+    const cuuint64_t strides[1] = {8 * sizeof(double)};
+    const cuuint32_t box[2] = {8, 1};
+    const cuuint32_t estr[2] = {1, 1};
+    CUresult r = encode(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, arrays[a], dims, strides, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(SPZ_ERR_CUDA, "cuTensorMapEncodeTiled failed");
+    static_assert(sizeof(CUtensorMap) == sizeof(h->tma_map[0]), "tensor map size");
+    std::memcpy(h->tma_map[a], &m, sizeof(m));
+  }
+  if (!h->tma_err) SPZ_CUDA(dev_alloc(&h->tma_err, sizeof(int)));
+  h->tma_ready = true;
+  return SPZ_OK;
+}
+
+// Blocks per SM of the TMA-staged kernel (per device and variant).
+int tma_launch_shape(int device, bool prefetch, int threads, size_t smem, int* resident_out) {
+  static std::mutex mu;
+  static int resident[kMaxDevices][2] = {};
+  if (device < 0 || device >= kMaxDevices) return fail(SPZ_ERR_INVALID_ARGUMENT, "device index out of range");
+  std::lock_guard<std::mutex> lock(mu);
+  int& r = resident[device][prefetch];
+  if (!r) {
+    const void* fn = prefetch ? (const void*)tile_kernel_tma<true> : (const void*)tile_kernel_tma<false>;
+    const int max_smem = (prefetch ? 4 : 2) * (8 << kTileMaxK) + (1 << (kTileMaxK - kTileLowBits)) * 8 + 128;
+    SPZ_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+    SPZ_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared));
+    int per_sm = 0;
+    SPZ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem));
+    r = std::max(1, per_sm);
+  }
+  *resident_out = r;
+  return SPZ_OK;
+}
+
 // Host arrays that one run of gates uploads from before it and downloads to
 // after it, with the copies overlapping the leading and the last tile passes
 // where a pass can be cut into kIoChunks slabs: slab j holds the amplitudes whose
@@ -761,6 +966,17 @@ int run_gates_io(spz_state_t h, const std::vector<GateApp>& gates_in, uint32_t f
     dtables = (const double2*)((char*)dscr + gbytes);
   }
 
+  // TMA staging (SPZ_EXEC_TMA*): tensor maps once per handle; the timeout word
+  // is cleared here and read back at the end of the run.
+  bool use_tma = false;
+#if !SPZ_TILE_SWIZZLE
+  if ((flags & (SPZ_EXEC_TMA | SPZ_EXEC_TMA_PREFETCH)) && n >= 5) {
+    int rc = ensure_tma_maps(h);
+    if (rc) return rc;
+    SPZ_CUDA(cudaMemsetAsync(h->tma_err, 0, sizeof(int), h->stream));
+    use_tma = true;
+  }
+#endif
   auto pass_slab_q = [&](const PlannedPass& P) -> int {
     if (!io || n < 3 || !tiled(P) || (n - P.local.size()) < 3) return -1;
     uint64_t local_mask = 0;
@@ -795,6 +1011,21 @@ int run_gates_io(spz_state_t h, const std::vector<GateApp>& gates_in, uint32_t f
     int resident = 0, sms = 0;
     int rc = tile_launch_shape(h->device, threads, smem, &resident, &sms);
     if (rc) return rc;
+    if (use_tma && A.c == kTileLowBits && A.k >= kTileLowBits + 2) {
+      const bool pre = (flags & SPZ_EXEC_TMA_PREFETCH) != 0;
+      const size_t tsmem = (pre ? 4 : 2) * T * sizeof(double) + (size_t)(1u << A.nhigh) * sizeof(uint64_t) + 128;
+      int tres = 0;
+      rc = tma_launch_shape(h->device, pre, threads, tsmem, &tres);
+      if (rc) return rc;
+      CUtensorMap mre, mim;
+      std::memcpy(&mre, h->tma_map[0], sizeof(mre));
+      std::memcpy(&mim, h->tma_map[1], sizeof(mim));
+      const uint64_t tblocks = std::min<uint64_t>(per, (uint64_t)sms * tres);
+      if (pre) tile_kernel_tma<true><<<(unsigned)tblocks, threads, tsmem, h->stream>>>(A, mre, mim, h->tma_err);
+      else tile_kernel_tma<false><<<(unsigned)tblocks, threads, tsmem, h->stream>>>(A, mre, mim, h->tma_err);
+      SPZ_CHECK_LAUNCH("tile_kernel_tma");
+      return SPZ_OK;
+    }
     const uint64_t blocks = std::min<uint64_t>(per, (uint64_t)sms * resident);
     tile_kernel<<<(unsigned)blocks, threads, smem, h->stream>>>(A);
     SPZ_CHECK_LAUNCH("tile_kernel");
@@ -906,7 +1137,14 @@ int run_gates_io(spz_state_t h, const std::vector<GateApp>& gates_in, uint32_t f
       st->bytes_moved += 32ull << n;
     }
   }
-  return timer.collect(st);
+  int rc = timer.collect(st);
+  if (!rc && use_tma) {
+    int bad = 0;
+    SPZ_CUDA(cudaMemcpyAsync(&bad, h->tma_err, sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+    SPZ_CUDA(cudaStreamSynchronize(h->stream));
+    if (bad) return fail(SPZ_ERR_TIMEOUT, "a TMA tile load did not complete within its wait limit");
+  }
+  return rc;
 }
 
 // Run a list of already validated gate applications on h.

@@ -86,6 +86,12 @@ struct spz_state_s {
   bool lazy = false;
   double factor_re = 1.0, factor_im = 0.0;
   int factor_exp = 0;
+  // TMA-staged tile passes (SPZ_EXEC_TMA*): tensor maps of re and im viewed as
+  // 2^(n-3) rows of 8 doubles (CUtensorMap, opaque 128 bytes each), built on
+  // first use, and a device word in which a timed-out wait is reported.
+  alignas(64) unsigned char tma_map[2][128] = {};
+  bool tma_ready = false;
+  int* tma_err = nullptr;
 };
 
 namespace spz {

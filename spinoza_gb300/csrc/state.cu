@@ -282,6 +282,7 @@ int spz_state_destroy(spz_state_t h) {
     cudaStreamDestroy(h->copy_stream);
   }
   if (h->meas) cudaFree(h->meas);
+  if (h->tma_err) cudaFree(h->tma_err);
   if (h->own_stream) cudaStreamDestroy(h->own_stream);
   delete h;
   return SPZ_OK;
