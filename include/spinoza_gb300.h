@@ -145,6 +145,14 @@ int spz_state_set_lazy(spz_state_t h, int enable);
  * there is none). */
 int spz_state_settle(spz_state_t h);
 
+/* Tile geometry of the fused passes that spz_circuit_execute,
+ * spz_circuit_execute_host and spz_iqft run on this handle: 2^tile_qubits
+ * amplitudes per shared-memory tile (4..10; 0 = 10) and threads per block
+ * (32 or 64; 0 = 64).  A tunable with no reference counterpart (the reference
+ * fixes its serial/parallel threshold, gates.rs:14): the exact mode's results
+ * are identical for every choice; the fast mode's equal up to rounding. */
+int spz_state_set_tile(spz_state_t h, int tile_qubits, int threads);
+
 /* --------------------------------------------------------- gate application */
 /* apply(gate, &mut State, target): uncontrolled gate.
  * Replaces spinoza/src/gates.rs:215-232.  SWAP takes its qubits from the gate

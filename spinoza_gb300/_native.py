@@ -131,6 +131,7 @@ SIGNATURES = [
     ("spz_state_fill_random", c_int, [c_void_p, c_uint64, c_int, c_int]),
     ("spz_state_set_lazy", c_int, [c_void_p, c_int]),
     ("spz_state_settle", c_int, [c_void_p]),
+    ("spz_state_set_tile", c_int, [c_void_p, c_int, c_int]),
     ("spz_apply", c_int, [c_void_p, POINTER(spz_gate), c_uint32]),
     ("spz_c_apply", c_int, [c_void_p, POINTER(spz_gate), c_uint32, c_uint32]),
     ("spz_cc_apply", c_int, [c_void_p, POINTER(spz_gate), c_uint32, c_uint32, c_uint32]),

@@ -405,3 +405,82 @@ def plan_stats(n: int, ops: np.ndarray, fused: bool = True, fast: bool = False) 
     flags = _flags(fused, fast)
     nat.check(nat.lib().spz_plan_stats(int(n), nat.ptr(ops), len(ops), flags, byref(st)))
     return {f: getattr(st, f) for f, _ in nat.spz_exec_stats._fields_}
+
+
+# ------------------------------------------------------------ executor tuning
+# (tile qubits, threads per block) of the fused passes.  Measured on the
+# 30-qubit brickwork (fast mode, share of the DFMA rate): 2^10 x 64 0.86,
+# 2^10 x 128 0.78, 2^9 x 64 0.80 (the executor's defaults are 2^10 x 64).
+EXECUTOR_CANDIDATES = [(10, 64), (10, 32), (9, 64), (9, 32), (8, 64)]
+
+
+def _executor_signature(n: int, ops: np.ndarray) -> str:
+    """Gate class x target class histogram of a circuit: the key its tuning is
+    cached under (dense / diagonal / measurement; 0, 1 or more controls;
+    target in the three low qubits, in a default tile, or above)."""
+    import hashlib
+
+    diag = {nat.Z, nat.P, nat.RZ}
+    hist = {}
+    for op in np.ascontiguousarray(ops, dtype=nat.OP_DTYPE):
+        kind = int(op["gate"]["kind"])
+        kc = "m" if kind == nat.M else ("d" if kind in diag else "x")
+        nc = bin(int(op["controls"])).count("1") if int(op["controls_kind"]) != nat.CONTROLS_NONE else 0
+        t = int(op["target"])
+        tc = "low" if t < 3 else ("tile" if t < 10 else "high")
+        key = f"{kc}{min(nc, 2)}{tc}"
+        hist[key] = hist.get(key, 0) + 1
+    text = ",".join(f"{k}:{hist[k]}" for k in sorted(hist))
+    return hashlib.sha256(f"{n}|{text}".encode()).hexdigest()[:16]
+
+
+def autotune_executor(state: State, ops: np.ndarray, fast: bool = False, candidates=EXECUTOR_CANDIDATES,
+                      reps: int = 2, use_cache: bool = True) -> dict:
+    """Pick the fused passes' tile geometry for running `ops` on `state`'s qubit
+    count: each candidate is timed (device time of the passes, mean of `reps`
+    runs from |0...0>; the state is overwritten), the fastest is set on the
+    state, and the choice is cached per GPU name, qubit count, mode and the
+    circuit's gate-class signature (SPZ_AUTOTUNE_CACHE or
+    ~/.cache/spinoza_gb300/executor_autotune.json)."""
+    import json
+    import os
+    from pathlib import Path
+
+    import torch
+
+    key = f"{torch.cuda.get_device_name()}|n={state.n}|fast={int(fast)}|{_executor_signature(state.n, ops)}"
+    base = os.environ.get("SPZ_AUTOTUNE_CACHE") or os.path.join(os.path.expanduser("~"), ".cache", "spinoza_gb300")
+    path = Path(base) / "executor_autotune.json"
+    cache = {}
+    if use_cache and path.exists():
+        try:
+            cache = json.loads(path.read_text())
+        except (OSError, ValueError):
+            cache = {}
+    if use_cache and key in cache:
+        best = cache[key]
+        state.set_tile(best["tile_qubits"], best["threads"])
+        return best
+    ops = np.ascontiguousarray(ops, dtype=nat.OP_DTYPE)
+    flags = (nat.EXEC_FAST if fast else nat.EXEC_DEFAULT) | nat.EXEC_TIME_PASSES
+    results = []
+    for k, t in candidates:
+        state.set_tile(k, t)
+        ms = 0.0
+        for r in range(reps + 1):  # the first run warms up
+            state.reset_zero()
+            tr, st = nat.spz_tracker(0, 0), nat.spz_exec_stats()
+            nat.check(nat.lib().spz_circuit_execute(state.handle, nat.ptr(ops), len(ops), byref(tr), flags, byref(st)))
+            if r:
+                ms += st.tile_ms + st.plain_ms
+        results.append({"tile_qubits": k, "threads": t, "ms": ms / reps})
+    best = dict(min(results, key=lambda r: r["ms"]), candidates=results)
+    state.set_tile(best["tile_qubits"], best["threads"])
+    if use_cache:
+        cache[key] = best
+        try:
+            path.parent.mkdir(parents=True, exist_ok=True)
+            path.write_text(json.dumps(cache, indent=1))
+        except OSError:
+            pass
+    return best

@@ -140,6 +140,12 @@ class State:
         """Fold the lazy mode's pending factor into the arrays now."""
         nat.check(nat.lib().spz_state_settle(self._h))
 
+    def set_tile(self, tile_qubits: int = 0, threads: int = 0) -> None:
+        """Tile geometry of this state's fused passes (spz_state_set_tile):
+        2^tile_qubits amplitudes (4..10) and 32 or 64 threads; 0 = defaults.
+        See spinoza_gb300.circuit.autotune_executor."""
+        nat.check(nat.lib().spz_state_set_tile(self._h, int(tile_qubits), int(threads)))
+
     def set_stream(self, stream) -> None:
         """Issue this state's work on `stream`: a torch.cuda.Stream, a raw
         cudaStream_t as int, or None for the handle's own stream.  torch's

@@ -705,7 +705,7 @@ uint64_t op_fp64_ops(uint32_t n, const GateApp& g, const std::vector<PhaseTable>
 int tile_launch_shape(int device, int threads, size_t smem, int* resident_out, int* sms_out) {
   static std::mutex mu;
   static int sms[kMaxDevices] = {};
-  static int resident[kMaxDevices][kTileMaxK + 2] = {};  // by log2 of the tile
+  static int resident[kMaxDevices][kTileMaxK + 2][2] = {};  // by log2 of the tile, and 32 / 64 threads
   if (device < 0 || device >= kMaxDevices) return fail(SPZ_ERR_INVALID_ARGUMENT, "device index out of range");
   std::lock_guard<std::mutex> lock(mu);
   if (!sms[device]) {
@@ -719,7 +719,7 @@ int tile_launch_shape(int device, int threads, size_t smem, int* resident_out, i
   }
   int lg = 0;  // the largest lg with 2 x 8 B x 2^lg <= smem (the tile's re and im)
   while (lg <= kTileMaxK && (16ull << (lg + 1)) <= smem) ++lg;
-  int& r = resident[device][lg];
+  int& r = resident[device][lg][threads > 32 ? 1 : 0];
   if (!r) {
     int per_sm = 0;
     SPZ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tile_kernel, threads, smem));
@@ -924,7 +924,7 @@ int run_gates_io(spz_state_t h, const std::vector<GateApp>& gates_in, uint32_t f
     }
     return timer.collect(st);
   }
-  const int k = std::min<int>((int)n, kTileMaxK);
+  const int k = std::min<int>((int)n, h->tile_k ? h->tile_k : kTileMaxK);
   const int c = std::min<int>(kTileLowBits, k);
   std::vector<PlannedPass> passes = plan(gates, n, k, c, !fast);
   // Phase tables, flattened (re, im) after the gate list.
@@ -1007,7 +1007,8 @@ int run_gates_io(spz_state_t h, const std::vector<GateApp>& gates_in, uint32_t f
     A.ngates = (int)P.gates.size();
     const uint32_t T = 1u << A.k;
     const size_t smem = 2 * T * sizeof(double) + (size_t)(1u << A.nhigh) * sizeof(uint64_t);
-    const int threads = (int)std::min<uint32_t>(kTileThreads, std::max<uint32_t>(32, T / 2));
+    const int threads = h->tile_threads ? h->tile_threads
+                                        : (int)std::min<uint32_t>(kTileThreads, std::max<uint32_t>(32, T / 2));
     int resident = 0, sms = 0;
     int rc = tile_launch_shape(h->device, threads, smem, &resident, &sms);
     if (rc) return rc;

@@ -92,6 +92,9 @@ struct spz_state_s {
   alignas(64) unsigned char tma_map[2][128] = {};
   bool tma_ready = false;
   int* tma_err = nullptr;
+  // Tile geometry of this handle's fused passes (spz_state_set_tile): log2 of
+  // the tile's amplitudes and threads per block; 0 = the library default.
+  int tile_k = 0, tile_threads = 0;
 };
 
 namespace spz {

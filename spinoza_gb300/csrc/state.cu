@@ -388,6 +388,17 @@ int spz_state_set_lazy(spz_state_t h, int enable) {
   return h->lazy ? SPZ_OK : settle(h);
 }
 
+int spz_state_set_tile(spz_state_t h, int tile_qubits, int threads) {
+  if (!h) return fail(SPZ_ERR_NULL, "handle is NULL");
+  if (tile_qubits != 0 && (tile_qubits < 4 || tile_qubits > 10))
+    return fail(SPZ_ERR_INVALID_ARGUMENT, "tile_qubits must be 0 or in 4..10");
+  if (threads != 0 && threads != 32 && threads != 64)
+    return fail(SPZ_ERR_INVALID_ARGUMENT, "threads must be 0, 32 or 64");
+  h->tile_k = tile_qubits;
+  h->tile_threads = threads;
+  return SPZ_OK;
+}
+
 int spz_state_settle(spz_state_t h) {
   if (!h) return fail(SPZ_ERR_NULL, "handle is NULL");
   return settle(h);
