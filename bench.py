@@ -850,8 +850,9 @@ def main() -> None:
     ap.add_argument("--batch-steps", type=int, default=1, help="timed runs of the config-5 batch")
     ap.add_argument("--batch-tpi", type=int, default=0, help="batch workload: tiles per work item of a wide instance")
     ap.add_argument("--batch-apart", action="store_true", help="batch workload: wide instances one at a time")
-    ap.add_argument("--batch-tile", type=int, default=11, help="batch workload: tile qubits (resident up to this n)")
-    ap.add_argument("--batch-threads", type=int, default=128, help="batch workload: threads per block")
+    ap.add_argument("--batch-tile", type=int, default=0,
+                    help="batch workload: tile qubits, resident up to this n (0: the library default)")
+    ap.add_argument("--batch-threads", type=int, default=0, help="batch workload: threads per block (0: default)")
     ap.add_argument("--batch-qmax", type=int, default=22, help="batch workload: largest instance (small profiling cases)")
     ap.add_argument("--batch-fast", action="store_true", help="batch workload: fast adjoint for the wide instances")
     ap.add_argument("--batch-wide", type=int, default=0,

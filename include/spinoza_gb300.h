@@ -390,8 +390,8 @@ typedef struct spz_batch_instance {
 } spz_batch_instance;
 
 typedef struct spz_batch_config {
-  int32_t tile_qubits;    /* local qubits per shared-memory tile, 4..12 (0 = 11) */
-  int32_t threads;        /* threads per CTA, multiple of 32 in 64..1024 (0 = 128) */
+  int32_t tile_qubits;    /* local qubits per shared-memory tile, 4..12 (0 = 9) */
+  int32_t threads;        /* threads per CTA, multiple of 32 in 64..1024 (0 = 64) */
   int32_t wide_qubits;    /* instances of at least this many qubits (and more than
                              tile_qubits) are split into work items across CTAs, each
                              with its own psi and lam in HBM; 0 = 18, > 30 = never.
@@ -403,7 +403,7 @@ typedef struct spz_batch_config {
                              across the GPU; SPZ_BATCH_WIDE_APART: the wide instances
                              run one at a time across the GPU in the exact mode too
                              (no per-instance workspace held for the whole run)      */
-  int32_t tiles_per_item; /* tiles per work item of a wide instance (0 = 16)       */
+  int32_t tiles_per_item; /* tiles per work item of a wide instance (0 = 64)       */
 } spz_batch_config;
 
 #define SPZ_BATCH_WIDE_APART 16

@@ -116,11 +116,10 @@ class Batch:
 
 
 # (tile qubits, threads per CTA, tiles per work item of a wide instance)
-# On the 4096-instance config-5 batch (one GB300, one box): 2^9 x 64 25.7 s,
-# 2^10 x 128 26.7 s, 2^11 x 128 28.2 s (wide instances as work items in the
-# launch).
-CANDIDATES = [(9, 64, 16), (9, 128, 16), (9, 64, 4), (9, 64, 64), (10, 64, 16), (10, 128, 16), (11, 128, 16),
-              (8, 64, 16)]
+# On the 4096-instance config-5 batch (one GB300, one box): 2^9 x 64 x 64
+# 25.65 s, x 16 25.71 s, 2^9 x 128 26.9 s, 2^10 x 128 26.7 s, 2^11 x 128
+# 28.2 s, 2^8 x 64 26.9 s (wide instances as work items in the launch).
+CANDIDATES = [(9, 64, 64), (9, 64, 16), (9, 128, 64), (10, 64, 64), (10, 128, 16), (11, 128, 16), (8, 64, 64)]
 
 
 def _signature(instances: Sequence[Instance]) -> str:

@@ -60,9 +60,10 @@ constexpr int kDefaultWideQubits = 18;
 #define SPZ_BATCH_WIDE_STREAMS 3
 #endif
 constexpr int kWideStreams = SPZ_BATCH_WIDE_STREAMS;
-// Tiles per work item of a wide instance (2^11-amplitude tiles: 16 tiles of a
-// 22-qubit pass make 128 items).
-constexpr int kDefaultTilesPerItem = 16;
+// Tiles per work item of a wide instance (2^9-amplitude tiles: 64 tiles of a
+// 22-qubit pass make 128 items).  Config 5 measured 25.65 s with 64, 25.71 s
+// with 16, 25.83 s with 4.
+constexpr int kDefaultTilesPerItem = 64;
 // Polls (about 0.3 us each) before a dependency wait gives up: far longer
 // than any item takes, short enough that a lost dependency ends the launch.
 constexpr unsigned long long kDefaultWaitPolls = 1ull << 24;
@@ -626,9 +627,10 @@ struct WideInst {
 
 struct BatchImpl {
   int device = 0;
-  // 2^11 tiles x 128 threads: 4096 instances of 10-17 qubits in 1.04 s, against
-  // 1.35-1.39 s with 2^12 x 256-512 and 1.60 s with 2^10 x 128.
-  int kmax = 11, threads = 128;
+  // 2^9 tiles x 64 threads (12 CTAs per SM): config 5 (4096 instances of 10-22
+  // qubits, the wide ones as work items) in 25.7 s, against 26.7 s with 2^10 x
+  // 128, 28.2 s with 2^11 x 128, 26.9 s with 2^9 x 128 and with 2^8 x 64.
+  int kmax = 9, threads = 64;
   int wide_qubits = kDefaultWideQubits;
   uint32_t wide_flags = 0;            // SPZ_EXEC_FAST: wide instances use the fast adjoint
   uint32_t nnarrow = 0;               // instances in the persistent kernel

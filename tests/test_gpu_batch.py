@@ -168,3 +168,16 @@ def test_autotuner_times_candidates_and_caches(gpu, tmp_path, monkeypatch):
     e, g = b.run()
     e1, g1 = _single(insts[5])
     assert abs(e[5] - e1) < 1e-12 * max(1.0, abs(e1))
+
+
+def test_batch_library_defaults_with_wide_items(gpu):
+    """The library's default launch shape (tile, threads, tiles per item) with
+    the 13- and 14-qubit instances as wide work items."""
+    insts = _instances()
+    b = batch.Batch(insts, wide_qubits=12)
+    assert b.info()["wide_in_kernel"] == 2
+    e, g = b.run()
+    for i in (4, 5, 2):
+        e1, g1 = _single(insts[i])
+        assert abs(e[i] - e1) < 1e-12 * max(1.0, abs(e1))
+        np.testing.assert_allclose(b.split(g)[i], g1, atol=1e-11, rtol=0)
