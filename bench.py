@@ -694,8 +694,11 @@ def batch_bench(args) -> dict:
     t0 = time.perf_counter()
     insts = batch.config5_instances(args.instances, qmax=args.batch_qmax)
     t_build = time.perf_counter() - t0
-    tune = (batch.autotune(insts, reps=1) if args.autotune
-            else {"tile_qubits": args.batch_tile, "threads": args.batch_threads, "tiles_per_item": args.batch_tpi})
+    explicit = args.batch_tile or args.batch_threads or args.batch_tpi
+    t0 = time.perf_counter()
+    tune = ({"tile_qubits": args.batch_tile, "threads": args.batch_threads, "tiles_per_item": args.batch_tpi}
+            if explicit or args.no_autotune else batch.autotune(insts, reps=1))
+    t_tune = time.perf_counter() - t0
     t0 = time.perf_counter()
     b = batch.Batch(insts, tile_qubits=tune["tile_qubits"], threads=tune["threads"], wide_qubits=args.batch_wide,
                     fast=args.batch_fast, tiles_per_item=tune.get("tiles_per_item", 0),
@@ -752,7 +755,7 @@ def batch_bench(args) -> dict:
             "max_abs_energy_diff_vs_loop": max_e, "max_abs_grad_diff_vs_loop": max_g,
             "max_abs_grad_diff_vs_oracle_parameter_shift": max_ps, "oracle_checks": checks,
             "oracle_instances": [int(insts[i][0]) for i in picks],
-            "build_seconds": t_build, "plan_seconds": t_plan, "info": b.info(),
+            "build_seconds": t_build, "plan_seconds": t_plan, "autotune_seconds": t_tune, "info": b.info(),
             "note": "loop = spz_adjoint_gradient per instance (fused executor, one instance at a time), timed on a "
                     "stratified sample and extrapolated; the batch is one graph launch (coefficients, the persistent "
                     "kernel with every instance, the fold of the wide instances' partial sums)"}
@@ -845,7 +848,8 @@ def main() -> None:
     ap.add_argument("--layers", type=int, default=20)
     ap.add_argument("--instances", type=int, default=4096)
     ap.add_argument("--loop-sample", type=int, default=64)
-    ap.add_argument("--autotune", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="batch: the library's default launch shape instead of the cached autotuner's choice")
     ap.add_argument("--no-batch", action="store_true", help="headline line without the config-5 batch object")
     ap.add_argument("--batch-steps", type=int, default=1, help="timed runs of the config-5 batch")
     ap.add_argument("--batch-tpi", type=int, default=0, help="batch workload: tiles per work item of a wide instance")
