@@ -107,6 +107,8 @@ int settle(spz_state_t h);
 void clear_factor(spz_state_t h);
 int scale_factor(spz_state_t h, double f_re, double f_im);
 int ensure_host_scratch(spz_state_t h, size_t bytes, void** out);
+// Copy kind for a caller's buffer moving into (to_device) or out of device memory.
+cudaMemcpyKind copy_kind(const void* p, bool to_device);
 int grid_for(uint64_t work, int threads = kThreads, int per_sm = 16);
 
 // ------------------------------------------------------ FP64 primitives

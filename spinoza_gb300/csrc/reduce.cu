@@ -836,7 +836,7 @@ int sample(spz_state_t h, const double* u, size_t nshots, uint64_t* out) {
   double* total = sb + nsuper;
   double* du = total + 8;
   uint64_t* dout = (uint64_t*)(du + nshots);
-  SPZ_CUDA(cudaMemcpyAsync(du, u, nshots * sizeof(double), cudaMemcpyDefault, h->stream));
+  SPZ_CUDA(cudaMemcpyAsync(du, u, nshots * sizeof(double), copy_kind(u, true), h->stream));
   const int cblocks = (int)std::min<uint64_t>((nchunks + 127) / 128, (uint64_t)kNumSMs * 16);
   chunk_total_kernel<<<cblocks, 128, 0, h->stream>>>(h->re, h->im, nchunks, cs, ss, ct, subs);
   super_total_kernel<<<(unsigned)((nsuper + 127) / 128), 128, 0, h->stream>>>(ct, nchunks, nsuper, st);
@@ -849,7 +849,7 @@ int sample(spz_state_t h, const double* u, size_t nshots, uint64_t* out) {
   rc = read_back(h, total, &host_total, 1);
   if (rc) return rc;
   if (!(host_total > 0.0)) return fail(SPZ_ERR_INVALID_ARGUMENT, "state has zero norm");
-  SPZ_CUDA(cudaMemcpyAsync(out, dout, nshots * sizeof(uint64_t), cudaMemcpyDefault, h->stream));
+  SPZ_CUDA(cudaMemcpyAsync(out, dout, nshots * sizeof(uint64_t), copy_kind(out, false), h->stream));
   SPZ_CUDA(cudaStreamSynchronize(h->stream));
   return SPZ_OK;
 }
