@@ -48,8 +48,9 @@ namespace {
 constexpr int kBatchMaxK = 12;
 constexpr int kBatchLowBits = 3;
 // Gradient accumulators per backward pass (passes with more parameters are
-// split); each warp keeps its own set in shared memory.
-constexpr int kMaxPassParams = 64;
+// split); each warp keeps its own set in shared memory.  48 keeps a 2^9-tile,
+// 64-thread CTA under 18 KiB of shared memory, so that 12 fit on an SM.
+constexpr int kMaxPassParams = 48;
 constexpr uint64_t kWorkspaceBudget = 128ull << 30;  // HBM for streamed instances' psi and lam
 // From about 2^18 amplitudes one instance (with two more running beside it on
 // other streams) keeps the GPU's block slots busy; below, one CTA per instance
@@ -274,13 +275,15 @@ struct BSmem {
 // bypass L1 (ld.global.cg): a wide instance's tiles are written by other CTAs.
 __device__ void run_pass(const BatchArgs& A, const BInst& I, const BPass& P, uint64_t t0, uint64_t t1, double* wpr,
                          double* wpi, double* wlr, double* wli, const BSmem& S, double* s_energy) {
+  const int K = P.k, C = P.c;
+  const uint32_t T = 1u << K;
   double* pr = S.pr;
-  double* pi = S.pi;
+  // A forward pass (psi only) may use a tile twice the shared-memory layout's:
+  // its imaginary parts then take the space of lam's real parts.
+  double* pi = K > A.kmax ? pr + T : S.pi;
   double* lr = S.lr;
   double* li = S.li;
   uint64_t* rowoff = S.rowoff;
-  const int K = P.k, C = P.c;
-  const uint32_t T = 1u << K;
   if (!I.resident) {
     for (uint32_t r = threadIdx.x; r < (1u << P.nhigh); r += blockDim.x) {
       uint64_t off = 0;
@@ -445,8 +448,8 @@ __global__ void __launch_bounds__(1024) batch_kernel(BatchArgs A) {
   S.lr = sm + 2 * TMAX;
   S.li = sm + 3 * TMAX;
   S.rowoff = reinterpret_cast<uint64_t*>(sm + 4 * TMAX);
-  S.red = sm + 4 * TMAX + (TMAX >> kBatchLowBits);
-  S.gacc = S.red + 64;
+  S.red = sm + 4 * TMAX + ((2 * TMAX) >> kBatchLowBits);  // after the row table (sized for forward tiles)
+  S.gacc = S.red + (blockDim.x >> 5);  // the block reduction needs one slot per warp
   __shared__ unsigned int s_next;
   __shared__ int s_flag;
   __shared__ double s_energy;
@@ -819,7 +822,8 @@ int build_batch(spz_batch_t b, const spz_batch_instance* inst, size_t ninst, con
     if (I.resident) {
       if (!fwd.empty()) fp.push_back(PlannedPass{all_local, fwd});
     } else {
-      fp = plan_passes(fwd, n, k, c);
+      // forward passes hold psi only, so their tiles may be twice as large
+      fp = plan_passes(fwd, n, std::min<int>((int)n, b->kmax + 1), c);
     }
     std::vector<GateApp> applied;  // in the order the passes apply them
     bool first = true;
@@ -1073,7 +1077,8 @@ int build_batch(spz_batch_t b, const spz_batch_instance* inst, size_t ninst, con
   SPZ_CUDA(host_alloc(&b->h_energy, std::max<size_t>(1, ninst) * sizeof(double)));
   // launch shape: persistent CTAs, as many per SM as shared memory allows
   const uint32_t TMAX = 1u << b->kmax;
-  b->smem = (4 * TMAX + (TMAX >> kBatchLowBits) + 64 + (size_t)(b->threads / 32) * kMaxPassParams) * sizeof(double);
+  b->smem = (4 * TMAX + ((2 * TMAX) >> kBatchLowBits) + (size_t)(b->threads / 32) * (1 + kMaxPassParams)) *
+            sizeof(double);
   SPZ_CUDA(cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem));
   int per_sm = 0;
   SPZ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel, b->threads, b->smem));
