@@ -692,7 +692,7 @@ def batch_bench(args) -> dict:
     from spinoza_gb300.core import State
 
     t0 = time.perf_counter()
-    insts = batch.config5_instances(args.instances, qmax=args.batch_qmax)
+    insts = batch.config5_instances(args.instances, qmin=args.batch_qmin, qmax=args.batch_qmax)
     t_build = time.perf_counter() - t0
     explicit = args.batch_tile or args.batch_threads or args.batch_tpi
     t0 = time.perf_counter()
@@ -744,7 +744,7 @@ def batch_bench(args) -> dict:
             checks += 1
     nparams = int(b.theta.size)
     qs = [x[0] for x in insts]
-    return {"workload": f"{len(insts)} HEA instances (RY/RZ layers + CZ ring), qubits U{{10..{args.batch_qmax}}}, "
+    return {"workload": f"{len(insts)} HEA instances (RY/RZ layers + CZ ring), qubits U{{{args.batch_qmin}..{args.batch_qmax}}}, "
                         f"depth U{{2..10}}, seeds 8+k", "instances": len(insts), "params": nparams,
             "qubits_min": min(qs), "qubits_max": max(qs), "launch": tune,
             "wide_qubits": args.batch_wide or 18, "wide_adjoint": "fast" if args.batch_fast else "exact",
@@ -858,6 +858,7 @@ def main() -> None:
                     help="batch workload: tile qubits, resident up to this n (0: the library default)")
     ap.add_argument("--batch-threads", type=int, default=0, help="batch workload: threads per block (0: default)")
     ap.add_argument("--batch-qmax", type=int, default=22, help="batch workload: largest instance (small profiling cases)")
+    ap.add_argument("--batch-qmin", type=int, default=10, help="batch workload: smallest instance (profiling cases)")
     ap.add_argument("--batch-fast", action="store_true", help="batch workload: fast adjoint for the wide instances")
     ap.add_argument("--batch-wide", type=int, default=0,
                     help="batch workload: instances of at least this many qubits run across the whole GPU "

@@ -57,10 +57,8 @@ constexpr uint64_t kWorkspaceBudget = 128ull << 30;  // HBM for streamed instanc
 // does better.  Config 5 (4096 instances of 10-22 qubits) measured 32.5 s with
 // the persistent kernel alone and 26.1-26.7 s with the threshold at 17-20.
 constexpr int kDefaultWideQubits = 18;
-#ifndef SPZ_BATCH_WIDE_STREAMS
-#define SPZ_BATCH_WIDE_STREAMS 3
-#endif
-constexpr int kWideStreams = SPZ_BATCH_WIDE_STREAMS;
+constexpr int kWideStreams = 4;         // at most this many wide instances in flight (whole-GPU path)
+constexpr int kDefaultWideStreams = 3;  // SPZ_BATCH_WIDE_STREAMS in the environment overrides it (1..4)
 // Tiles per work item of a wide instance (2^9-amplitude tiles: 64 tiles of a
 // 22-qubit pass make 128 items).  Config 5 measured 25.65 s with 64, 25.71 s
 // with 16, 25.83 s with 4.
@@ -206,55 +204,122 @@ __device__ void b_apply(const BGate& g, uint64_t base, double* re, double* im, u
   }
 }
 
-// This thread's share of Im<lam| Pi sigma |psi> over the gate's amplitudes in
-// the tile.  X and Y generators pair s0 with s1 (the target is local); the
-// diagonal generators (Z for RZ, |1><1| for P) are elementwise,
-// sum over x of +-Im(conj(lam_x) psi_x), with the target bit read from the
-// element or, for a non-local target, from the tile base.
-template <int NPOS>
-__device__ __forceinline__ double b_grad_part_n(const BGate& g, uint64_t base, const double* pr, const double* pi,
-                                                const double* lr, const double* li, uint32_t nw) {
+// Backward step of one gate on a tile, in one loop over the gate's pairs (or
+// elements): this thread's share of the gradient term Im<lam| Pi sigma |psi>
+// when the gate carries a parameter, taken from psi and lam as they are before
+// the step, then the inverse gate (the descriptor already holds it) on both.
+// X and Y generators pair s0 with s1 (the target is local); the diagonal
+// generators (Z for RZ, |1><1| for P) are elementwise, sum over x of
+// +-Im(conj(lam_x) psi_x), with the target bit read from the element or, for a
+// non-local target, from the tile base (gone).
+template <int KIND, int NPOS>
+__device__ __forceinline__ double b_bwd_pair(const BGate& g, double* pr, double* pi, double* lr, double* li,
+                                             uint32_t nw) {
   const Enumerator<NPOS, BGate> E(g);
   const uint32_t tbit = g.tbit;
+  const Coef cf = g.c;
   const int grad = g.grad;
   double acc = 0.0;
-  if (g.mode != BM_PAIR) {
-    const int gone = g.mode == BM_DIAG_GLOBAL ? ((base & g.g_tbit) ? 1 : 0) : -1;
-    if (grad == BG_P1 && gone == 0) return 0.0;
-    for (uint32_t m = threadIdx.x; m < nw; m += blockDim.x) {
-      const uint32_t e = E(m);
-      const bool one = gone >= 0 ? gone != 0 : (e & tbit) != 0;
-      if (grad == BG_P1 && !one) continue;
-      const double v = dfma(lr[e], pi[e], dmul(dneg(li[e]), pr[e]));  // Im(conj(lam) psi)
-      acc = (grad == BG_Z && one) ? dsub(acc, v) : dadd(acc, v);
-    }
-    return acc;
-  }
   for (uint32_t m = threadIdx.x; m < nw; m += blockDim.x) {
-    const uint32_t s0 = E(m);
-    const uint32_t s1 = s0 | tbit;
-    const double a = pr[s0], b = pi[s0], c = pr[s1], d = pi[s1];
-    const double p = lr[s0], q = li[s0], r = lr[s1], s = li[s1];
-    double v;
-    switch (grad) {
-      case BG_X: v = dadd(dfma(p, d, dmul(dneg(q), c)), dfma(r, b, dmul(dneg(s), a))); break;
-      case BG_Y: v = dsub(dfma(r, a, dmul(s, b)), dfma(p, c, dmul(q, d))); break;
-      case BG_Z: v = dsub(dfma(p, b, dmul(dneg(q), a)), dfma(r, d, dmul(dneg(s), c))); break;
-      default: v = dfma(r, d, dmul(dneg(s), c)); break;
+    const uint32_t s0 = E(m), s1 = s0 | tbit;
+    double a = pr[s0], b = pi[s0], c = pr[s1], d = pi[s1];
+    double p = lr[s0], q = li[s0], r = lr[s1], s = li[s1];
+    if (grad != BG_NONE) {
+      double v;
+      switch (grad) {
+        case BG_X: v = dadd(dfma(p, d, dmul(dneg(q), c)), dfma(r, b, dmul(dneg(s), a))); break;
+        case BG_Y: v = dsub(dfma(r, a, dmul(s, b)), dfma(p, c, dmul(q, d))); break;
+        case BG_Z: v = dsub(dfma(p, b, dmul(dneg(q), a)), dfma(r, d, dmul(dneg(s), c))); break;
+        default: v = dfma(r, d, dmul(dneg(s), c)); break;
+      }
+      acc = dadd(acc, v);
     }
-    acc = dadd(acc, v);
+    gate_pair<KIND>(cf, a, b, c, d);
+    gate_pair<KIND>(cf, p, q, r, s);
+    pr[s0] = a; pi[s0] = b; pr[s1] = c; pi[s1] = d;
+    lr[s0] = p; li[s0] = q; lr[s1] = r; li[s1] = s;
   }
   return acc;
 }
 
-__device__ double b_grad_part(const BGate& g, uint64_t base, const double* pr, const double* pi, const double* lr,
-                              const double* li, uint32_t T) {
-  const uint32_t nw = T >> g.npos;
+template <int KIND, int NPOS>
+__device__ __forceinline__ double b_bwd_diag(const BGate& g, int gone, double* pr, double* pi, double* lr, double* li,
+                                             uint32_t nw) {
+  const Enumerator<NPOS, BGate> E(g);
+  const uint32_t tbit = g.tbit;
+  const Coef cf = g.c;
+  const int grad = g.grad;
+  double acc = 0.0;
+  for (uint32_t m = threadIdx.x; m < nw; m += blockDim.x) {
+    const uint32_t e = E(m);
+    const bool one = gone >= 0 ? gone != 0 : (e & tbit) != 0;
+    double a = pr[e], b = pi[e], p = lr[e], q = li[e];
+    if (grad != BG_NONE && !(grad == BG_P1 && !one)) {
+      const double v = dfma(p, b, dmul(dneg(q), a));  // Im(conj(lam) psi)
+      acc = (grad == BG_Z && one) ? dsub(acc, v) : dadd(acc, v);
+    }
+    gate_diag<KIND>(cf, one, a, b);
+    gate_diag<KIND>(cf, one, p, q);
+    pr[e] = a; pi[e] = b; lr[e] = p; li[e] = q;
+  }
+  return acc;
+}
+
+template <int KIND>
+__device__ __forceinline__ double b_bwd_pair_any(const BGate& g, double* pr, double* pi, double* lr, double* li,
+                                                 uint32_t nw) {
   double r = 0.0;
-#define SPZ_CALL(N) r = b_grad_part_n<N>(g, base, pr, pi, lr, li, nw)
+#define SPZ_CALL(N) r = b_bwd_pair<KIND, N>(g, pr, pi, lr, li, nw)
   SPZ_BY_NPOS(g.npos, SPZ_CALL)
 #undef SPZ_CALL
   return r;
+}
+
+template <int KIND>
+__device__ __forceinline__ double b_bwd_diag_any(const BGate& g, int gone, double* pr, double* pi, double* lr,
+                                                 double* li, uint32_t nw) {
+  double r = 0.0;
+#define SPZ_CALL(N) r = b_bwd_diag<KIND, N>(g, gone, pr, pi, lr, li, nw)
+  SPZ_BY_NPOS(g.npos, SPZ_CALL)
+#undef SPZ_CALL
+  return r;
+}
+
+// This thread's gradient share of gate g on the tile, with g applied to psi and lam.
+__device__ double b_bwd_gate(const BGate& g, uint64_t base, double* pr, double* pi, double* lr, double* li,
+                             uint32_t T) {
+  const uint32_t nw = T >> g.npos;
+  double v = 0.0;
+  switch (g.mode) {
+    case BM_PAIR:
+      switch (g.kind) {
+        case SPZ_GATE_H: v = b_bwd_pair_any<SPZ_GATE_H>(g, pr, pi, lr, li, nw); break;
+        case SPZ_GATE_X: v = b_bwd_pair_any<SPZ_GATE_X>(g, pr, pi, lr, li, nw); break;
+        case SPZ_GATE_Y: v = b_bwd_pair_any<SPZ_GATE_Y>(g, pr, pi, lr, li, nw); break;
+        case SPZ_GATE_RX: v = b_bwd_pair_any<SPZ_GATE_RX>(g, pr, pi, lr, li, nw); break;
+        case SPZ_GATE_RY: v = b_bwd_pair_any<SPZ_GATE_RY>(g, pr, pi, lr, li, nw); break;
+        default: v = b_bwd_pair_any<SPZ_GATE_U>(g, pr, pi, lr, li, nw); break;
+      }
+      break;
+    case BM_DIAG_LOCAL:
+    case BM_DIAG_GLOBAL: {
+      int gone = -1;
+      if (g.mode == BM_DIAG_GLOBAL) {
+        gone = (base & g.g_tbit) ? 1 : 0;
+        if (!gone && g.kind != SPZ_GATE_RZ) break;  // Z / P (and the P1 gradient) live on the 1 half
+      }
+      switch (g.kind) {
+        case SPZ_GATE_Z: v = b_bwd_diag_any<SPZ_GATE_Z>(g, gone, pr, pi, lr, li, nw); break;
+        case SPZ_GATE_P: v = b_bwd_diag_any<SPZ_GATE_P>(g, gone, pr, pi, lr, li, nw); break;
+        default: v = b_bwd_diag_any<SPZ_GATE_RZ>(g, gone, pr, pi, lr, li, nw); break;
+      }
+      break;
+    }
+    default:
+      tile_swap_any(g, pr, pi, nw);
+      tile_swap_any(g, lr, li, nw);
+  }
+  return v;
 }
 
 __device__ __forceinline__ uint64_t b_global(uint64_t base, const uint64_t* rowoff, uint32_t e, int c) {
@@ -362,15 +427,11 @@ __device__ void run_pass(const BatchArgs& A, const BInst& I, const BPass& P, uin
       for (uint32_t gi = 0; gi < P.gate_count; ++gi) {
         const BGate& g = A.gates[P.gate_begin + gi];
         if ((base & g.g_ones) != g.g_ones || (base & g.g_zeros) != 0) continue;
-        if (g.grad != BG_NONE) {
-          // this warp's share, into its own accumulator (no block reduction per tile)
-          double part = b_grad_part(g, base, pr, pi, lr, li, T);
+        double part = b_bwd_gate(g, base, pr, pi, lr, li, T);
+        if (g.grad != BG_NONE) {  // uniform: this warp's share, into its own accumulator
           for (int off = 16; off > 0; off >>= 1) part = dadd(part, __shfl_down_sync(0xffffffffu, part, off));
           if (lane == 0) S.gacc[warp * kMaxPassParams + g.gacc] = dadd(S.gacc[warp * kMaxPassParams + g.gacc], part);
-          __syncthreads();  // every read of psi and lam for the gradient precedes the update
         }
-        b_apply(g, base, pr, pi, T);
-        b_apply(g, base, lr, li, T);
         __syncthreads();
       }
     }
@@ -439,7 +500,22 @@ __device__ bool wait_until(const BatchArgs& A, const unsigned int* ctr, unsigned
   return ok;
 }
 
-__global__ void __launch_bounds__(1024) batch_kernel(BatchArgs A) {
+// Copy a pass descriptor to shared memory, so that the pass reads it without
+// global loads after every block barrier.  Barriers on both sides: the previous
+// pass's readers are done before it is overwritten.
+__device__ __forceinline__ const BPass& stage_pass(const BPass* src, BPass* dst) {
+  static_assert(sizeof(BPass) % 4 == 0, "BPass is copied as 32-bit words");
+  __syncthreads();
+  if (threadIdx.x < sizeof(BPass) / 4)
+    reinterpret_cast<uint32_t*>(dst)[threadIdx.x] = reinterpret_cast<const uint32_t*>(src)[threadIdx.x];
+  __syncthreads();
+  return *dst;
+}
+
+// Instantiated for the default 64-thread CTAs (12 per SM: up to 85 registers
+// a thread) and for CTAs of up to 1024 threads (64 registers a thread).
+template <int MAXT, int MINB>
+__global__ void __launch_bounds__(MAXT, MINB) batch_kernel(BatchArgs A) {
   extern __shared__ double sm[];
   const uint32_t TMAX = 1u << A.kmax;
   BSmem S;
@@ -453,6 +529,7 @@ __global__ void __launch_bounds__(1024) batch_kernel(BatchArgs A) {
   __shared__ unsigned int s_next;
   __shared__ int s_flag;
   __shared__ double s_energy;
+  __shared__ BPass s_pass;
   const uint64_t wsN = 1ull << A.ws_qubits;
   double* wpr = A.workspace ? A.workspace + (uint64_t)blockIdx.x * 4 * wsN : nullptr;
   double* wpi = wpr ? wpr + wsN : nullptr;
@@ -471,7 +548,7 @@ __global__ void __launch_bounds__(1024) batch_kernel(BatchArgs A) {
     __syncthreads();
     if (W.pass == kWholeInstance) {
       for (uint32_t pidx = 0; pidx < I.npass; ++pidx) {
-        const BPass& P = A.passes[I.pass_begin + pidx];
+        const BPass& P = stage_pass(A.passes + I.pass_begin + pidx, &s_pass);
         run_pass(A, I, P, 0, 1ull << (I.n - P.k), wpr, wpi, wlr, wli, S, &s_energy);
         if (P.kind == BP_BWD) {
           for (uint32_t gi = threadIdx.x; gi < P.gate_count; gi += blockDim.x) {
@@ -490,7 +567,7 @@ __global__ void __launch_bounds__(1024) batch_kernel(BatchArgs A) {
     }
     // one pass of a wide instance over a tile range
     if (!wait_until(A, A.done + I.wide, W.need, &s_flag)) break;
-    const BPass& P = A.passes[I.pass_begin + W.pass];
+    const BPass& P = stage_pass(A.passes + I.pass_begin + W.pass, &s_pass);
     const uint64_t N = 1ull << I.n;
     double* ipr = A.wide_ws + I.ws_offset;
     run_pass(A, I, P, W.tile_begin, W.tile_end, ipr, ipr + N, ipr + 2 * N, ipr + 3 * N, S, &s_energy);
@@ -519,6 +596,10 @@ __global__ void batch_fold_kernel(const BSum* __restrict__ sums, uint32_t nsums,
   v = dmul(f.factor, v);
   if (f.energy) energies[f.out] = v;
   else grads[f.out] = v;
+}
+
+const void* batch_kernel_fn(int threads) {
+  return threads <= 64 ? (const void*)batch_kernel<64, 12> : (const void*)batch_kernel<1024, 1>;
 }
 
 // Coefficients of every parameterised gate from the current angles.
@@ -641,6 +722,7 @@ struct BatchImpl {
   // Wide instances run on kWideStreams streams at once (a pass of one 20-22
   // qubit instance leaves block slots empty; another instance fills them),
   // each stream with its own state per size (lazily created).
+  int wide_streams = kDefaultWideStreams;
   cudaStream_t wide_stream[kWideStreams] = {};
   cudaEvent_t wide_done[kWideStreams] = {};
   spz_state_t wide_h[kWideStreams][31] = {};
@@ -1079,9 +1161,10 @@ int build_batch(spz_batch_t b, const spz_batch_instance* inst, size_t ninst, con
   const uint32_t TMAX = 1u << b->kmax;
   b->smem = (4 * TMAX + ((2 * TMAX) >> kBatchLowBits) + (size_t)(b->threads / 32) * (1 + kMaxPassParams)) *
             sizeof(double);
-  SPZ_CUDA(cudaFuncSetAttribute(batch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem));
+  const void* kfn = batch_kernel_fn(b->threads);
+  SPZ_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)b->smem));
   int per_sm = 0;
-  SPZ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, batch_kernel, b->threads, b->smem));
+  SPZ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kfn, b->threads, b->smem));
   if (per_sm < 1) return fail(SPZ_ERR_UNSUPPORTED, "batch kernel does not fit on an SM with this configuration");
   int sms = 0;
   SPZ_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, b->device));
@@ -1128,7 +1211,10 @@ int capture_graph(spz_batch_t b) {
   A.ws_qubits = b->ws_qubits;
   A.counter = b->d_counter;
   A.kmax = b->kmax;
-  if (b->nitems) batch_kernel<<<b->grid, b->threads, b->smem, b->stream>>>(A);
+  if (b->nitems) {
+    if (b->threads <= 64) batch_kernel<64, 12><<<b->grid, b->threads, b->smem, b->stream>>>(A);
+    else batch_kernel<1024, 1><<<b->grid, b->threads, b->smem, b->stream>>>(A);
+  }
   if (b->nsums)
     batch_fold_kernel<<<(b->nsums + 255) / 256, 256, 0, b->stream>>>(b->d_sums, b->nsums, b->d_partials, b->d_energy,
                                                                      b->d_grad);
@@ -1160,6 +1246,10 @@ int spz_batch_create(const spz_batch_instance* instances, size_t ninstances, con
     if (config->wide_qubits) b->wide_qubits = config->wide_qubits;
     b->wide_flags = (uint32_t)config->flags & (SPZ_EXEC_FAST | SPZ_BATCH_WIDE_APART);
     if (config->tiles_per_item) b->tiles_per_item = config->tiles_per_item;
+  }
+  {
+    const char* v = std::getenv("SPZ_BATCH_WIDE_STREAMS");
+    if (v && v[0] >= '1' && v[0] <= '0' + kWideStreams && v[1] == 0) b->wide_streams = v[0] - '0';
   }
   {  // host-side fault injection for tests: wide items wait on counts never reached
     const char* v = std::getenv("SPZ_BATCH_TEST_STALL");
@@ -1208,7 +1298,7 @@ int spz_batch_run(spz_batch_t b, const double* theta, double* energies, double* 
   };
   for (size_t wi = 0; wi < b->wide.size(); ++wi) {
     WideInst& w = b->wide[wi];
-    const int si = (int)(wi % kWideStreams);
+    const int si = (int)(wi % (size_t)b->wide_streams);
     if (!b->wide_stream[si]) {
       SPZ_CUDA(cudaStreamCreateWithFlags(&b->wide_stream[si], cudaStreamNonBlocking));
       SPZ_CUDA(cudaEventCreateWithFlags(&b->wide_done[si], cudaEventDisableTiming));
