@@ -1,7 +1,7 @@
 #!/usr/bin/env python3
 """Benchmark: 30-qubit FP64 brickwork circuit on one GB300 (+ adjoint gradients).
 
-Workload (config 2, the brickwork circuit): 30 qubits FP64 (16 GiB state), from |0...0>,
+Workload (the brickwork circuit): 30 qubits FP64 (16 GiB state), from |0...0>,
 20 layers of U(theta, phi, lambda) on every qubit (angles uniform in [0, 2 pi)
 from the seeded splitmix64 stream, seed 2), then CX on (0,1),(2,3),...,(28,29)
 and (1,2),...,(27,28): 1180 gates.  One step = reset to |0...0> + execute the
@@ -236,7 +236,7 @@ def reference_arm(args) -> None:
 
 # ---------------------------------------------------------------- GPU arm
 def adjoint_bench(n: int = 24, layers: int = 8, fd_sample: int = 4) -> dict:
-    """Config 4: adjoint gradient of the 384-parameter ansatz vs central FD
+    """Adjoint gradient of the 24-qubit, 384-parameter ansatz vs central FD
     (768 forward circuits) with the plain per-gate kernels, same GPU."""
     import torch
 
@@ -595,7 +595,7 @@ def _event_time(fn, steps: int, warmup: int) -> float:
 
 
 def workload_qft20(args) -> None:
-    """Config 1: QFT with swaps on a seeded N(0,1) normalised 20-qubit state."""
+    """QFT with swaps on a seeded N(0,1) normalised 20-qubit state."""
     import oracle
     from spinoza_gb300 import _native as nat
     from spinoza_gb300 import circuit, rng
@@ -646,7 +646,7 @@ def workload_qft20(args) -> None:
     d_fast = float(max(np.max(np.abs(gre - re)), np.max(np.abs(gim - im))))
     d = float(max(np.max(np.abs(pre - re)), np.max(np.abs(pim - im))))
     abytes = algorithmic_bytes(ops, n)
-    _line("config1 QFT-20 circuit time", out["program_fast"] * 1e3, "ms", args, higher_is_better=False,
+    _line("QFT-20 circuit time", out["program_fast"] * 1e3, "ms", args, higher_is_better=False,
           config={"workload": "QFT with swaps, 20 qubits, N(0,1) normalised state seed 1", "gates": len(ops)},
           execute_ms=out["fused"] * 1e3, unfused_ms=out["unfused"] * 1e3,
           effective_gbs=abytes / out["program_fast"] / 1e9,
@@ -659,7 +659,7 @@ def workload_qft20(args) -> None:
 
 
 def workload_measure28(args) -> None:
-    """Config 3: 28 qubits, 1e6 seeded shots (bit-exact rule) and <H> = sum a ZZ + b X."""
+    """28 qubits: 1e6 seeded shots (bit-exact rule) and <H> = sum a ZZ + b X."""
     from spinoza_gb300 import core, rng
     from spinoza_gb300.core import State
 
@@ -674,7 +674,7 @@ def workload_measure28(args) -> None:
     H = core.ising_hamiltonian(a, b)
     t_h = _event_time(lambda: core.pauli_expectation(s, H), args.steps, 1)
     N = 1 << n
-    _line("config3 shots/s at 28 qubits", 1e6 / t_shots, "shots/s", args, higher_is_better=True,
+    _line("shots/s at 28 qubits", 1e6 / t_shots, "shots/s", args, higher_is_better=True,
           config={"workload": "28-qubit N(0,1) normalised state, 1e6 shots (uniform seed 4), <H> with "
                               "a_i, b_i ~ N(0,1) (seed 5)", "terms": int(len(H))},
           sample_ms=t_shots * 1e3, sample_gbs=(24 * N) / t_shots / 1e9, expectation_ms=t_h * 1e3,
@@ -682,7 +682,7 @@ def workload_measure28(args) -> None:
 
 
 def batch_bench(args) -> dict:
-    """Config 5: 4096 instances, qubits 10..22, depth 2..10, forward <H> and
+    """4096 variational instances, qubits 10..22, depth 2..10, forward <H> and
     adjoint gradients of all of them per graph launch, against a loop of the
     single-instance path (spz_adjoint_gradient, one instance at a time) on a
     stratified sample, and against the oracle's parameter shift on sampled
@@ -692,7 +692,7 @@ def batch_bench(args) -> dict:
     from spinoza_gb300.core import State
 
     t0 = time.perf_counter()
-    insts = batch.config5_instances(args.instances, qmin=args.batch_qmin, qmax=args.batch_qmax)
+    insts = batch.hea_workload(args.instances, qmin=args.batch_qmin, qmax=args.batch_qmax)
     t_build = time.perf_counter() - t0
     explicit = args.batch_tile or args.batch_threads or args.batch_tpi
     t0 = time.perf_counter()
@@ -763,7 +763,7 @@ def batch_bench(args) -> dict:
 
 def workload_batch(args) -> None:
     d = batch_bench(args)
-    _line("config5 batched forward+adjoint instances/s", d["instances_per_s"], "instances/s", args,
+    _line("batched forward+adjoint instances/s", d["instances_per_s"], "instances/s", args,
           higher_is_better=True, config={"workload": d["workload"], "params": d["params"], "launch": d["launch"]},
           batch=d)
 
@@ -796,7 +796,7 @@ def workload_gate(args) -> None:
 
 
 def workload_sweep33(args) -> None:
-    """Config 2 sweep: H, RZ, CX and 3-control X on every target at 33 qubits (128 GiB)."""
+    """Per-gate sweep: H, RZ, CX and 3-control X on every target at 33 qubits (128 GiB)."""
     import torch
 
     from spinoza_gb300 import gates as G
@@ -827,7 +827,7 @@ def workload_sweep33(args) -> None:
                          "gbs_median": statistics.median(x["gbs"] for x in r),
                          "frac_median": statistics.median(x["frac"] for x in r),
                          "frac_min": min(x["frac"] for x in r)}
-    _line(f"config2 per-gate sweep at {n} qubits", summary["H"]["gbs_median"], "GB/s", args, higher_is_better=True,
+    _line(f"per-gate sweep at {n} qubits", summary["H"]["gbs_median"], "GB/s", args, higher_is_better=True,
           config={"workload": f"H, RZ(0.7), CX(control (t+1) mod n), X with 3 controls (t+1..t+3 mod n), "
                               f"targets 0..{n - 1}, {n} qubits ({16 * N >> 30} GiB)"},
           summary=summary, rows=rows, peak_gbs=peaks["hbm_gbs"])
@@ -850,8 +850,8 @@ def main() -> None:
     ap.add_argument("--loop-sample", type=int, default=64)
     ap.add_argument("--no-autotune", action="store_true",
                     help="batch: the library's default launch shape instead of the cached autotuner's choice")
-    ap.add_argument("--no-batch", action="store_true", help="headline line without the config-5 batch object")
-    ap.add_argument("--batch-steps", type=int, default=1, help="timed runs of the config-5 batch")
+    ap.add_argument("--no-batch", action="store_true", help="headline line without the 4096-instance batch object")
+    ap.add_argument("--batch-steps", type=int, default=1, help="timed runs of the 4096-instance batch")
     ap.add_argument("--batch-tpi", type=int, default=0, help="batch workload: tiles per work item of a wide instance")
     ap.add_argument("--batch-apart", action="store_true", help="batch workload: wide instances one at a time")
     ap.add_argument("--batch-tile", type=int, default=0,

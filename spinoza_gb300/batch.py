@@ -2,7 +2,7 @@
 independent circuits of uneven qubit counts in one persistent, graph-replayed
 launch (spz_batch_*).  No reference counterpart (new form).
 
-``config5_instances`` builds the seeded workload of BASELINE config 5
+``hea_workload`` builds the seeded variational workload
 (4096 hardware-efficient ansatz instances, qubits uniform in 10..22, depth
 uniform in 2..10, RY/RZ layers + CZ ring, observable sum a_i Z_i Z_{i+1} + b_i X_i).
 ``autotune`` times candidate launch shapes (tile qubits x threads per CTA) and
@@ -40,7 +40,7 @@ def hea_instance(n: int, depth: int, seed: int) -> Instance:
     return n, ops, pidx, theta, ising_hamiltonian(a, b)
 
 
-def config5_instances(count: int = 4096, qmin: int = 10, qmax: int = 22, dmin: int = 2, dmax: int = 10,
+def hea_workload(count: int = 4096, qmin: int = 10, qmax: int = 22, dmin: int = 2, dmax: int = 10,
                       base_seed: int = 8) -> List[Instance]:
     """Qubits uniform in qmin..qmax and depth uniform in dmin..dmax from stream
     `base_seed`; instance k draws its angles and observable from seed base_seed + k."""
@@ -116,7 +116,7 @@ class Batch:
 
 
 # (tile qubits, threads per CTA, tiles per work item of a wide instance)
-# On the 4096-instance config-5 batch (one GB300, one box): 2^9 x 64 x 64
+# On the 4096-instance, 10-22-qubit batch (one GB300, one box): 2^9 x 64 x 64
 # 25.65 s, x 16 25.71 s, 2^9 x 128 26.9 s, 2^10 x 128 26.7 s, 2^11 x 128
 # 28.2 s, 2^8 x 64 26.9 s (wide instances as work items in the launch).
 CANDIDATES = [(9, 64, 64), (9, 64, 16), (9, 128, 64), (10, 64, 64), (10, 128, 16), (11, 128, 16), (8, 64, 64)]

@@ -54,13 +54,14 @@ constexpr int kMaxPassParams = 48;
 constexpr uint64_t kWorkspaceBudget = 128ull << 30;  // HBM for streamed instances' psi and lam
 // From about 2^18 amplitudes one instance (with two more running beside it on
 // other streams) keeps the GPU's block slots busy; below, one CTA per instance
-// does better.  Config 5 (4096 instances of 10-22 qubits) measured 32.5 s with
+// does better.  4096 instances of 10-22 qubits measured 32.5 s with
 // the persistent kernel alone and 26.1-26.7 s with the threshold at 17-20.
 constexpr int kDefaultWideQubits = 18;
 constexpr int kWideStreams = 4;         // at most this many wide instances in flight (whole-GPU path)
 constexpr int kDefaultWideStreams = 3;  // SPZ_BATCH_WIDE_STREAMS in the environment overrides it (1..4)
 // Tiles per work item of a wide instance (2^9-amplitude tiles: 64 tiles of a
-// 22-qubit pass make 128 items).  Config 5 measured 25.65 s with 64, 25.71 s
+// 22-qubit pass make 128 items).  The 4096-instance batch of 10-22 qubits
+// measured 25.65 s with 64, 25.71 s
 // with 16, 25.83 s with 4.
 constexpr int kDefaultTilesPerItem = 64;
 // Polls (about 0.3 us each) before a dependency wait gives up: far longer
@@ -711,7 +712,7 @@ struct WideInst {
 
 struct BatchImpl {
   int device = 0;
-  // 2^9 tiles x 64 threads (12 CTAs per SM): config 5 (4096 instances of 10-22
+  // 2^9 tiles x 64 threads (12 CTAs per SM): the batch of 4096 instances of 10-22
   // qubits, the wide ones as work items) in 25.7 s, against 26.7 s with 2^10 x
   // 128, 28.2 s with 2^11 x 128, 26.9 s with 2^9 x 128 and with 2^8 x 64.
   int kmax = 9, threads = 64;

@@ -145,8 +145,8 @@ def test_batch_rejects_bad_input(gpu):
         batch.Batch([(n, ops, bad, theta, terms)])
 
 
-def test_config5_generator_shapes():
-    insts = batch.config5_instances(count=64)
+def test_variational_workload_shapes():
+    insts = batch.hea_workload(count=64)
     qs = [i[0] for i in insts]
     assert min(qs) >= 10 and max(qs) <= 22
     for n, ops, pidx, theta, terms in insts:

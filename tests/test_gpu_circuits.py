@@ -42,7 +42,7 @@ def _builder():
 
 
 def qft_with_swaps(n):
-    """Config 1: for j = n-1..0: H(j), CP(pi/2^(j-k)) k < j; then SWAP(i, n-1-i)."""
+    """QFT with swaps: for j = n-1..0: H(j), CP(pi/2^(j-k)) k < j; then SWAP(i, n-1-i)."""
     qc = _builder()
     for j in range(n - 1, -1, -1):
         qc.h(j)
@@ -54,7 +54,7 @@ def qft_with_swaps(n):
 
 
 def brickwork(n, layers, seed=2):
-    """Config 2 shape: U(theta, phi, lambda) on every qubit, then CX even, CX odd."""
+    """Brickwork: U(theta, phi, lambda) on every qubit, then CX even, CX odd."""
     qc = _builder()
     ang = rng.uniforms(seed, 3 * n * layers) * 2 * math.pi
     k = 0
@@ -99,8 +99,8 @@ def _compare(a, b, exact=True):
         assert np.array_equal(gre, ore) and np.array_equal(gim, oim), d
 
 
-def test_qft20_config1_parity(gpu):
-    """Config 1: QFT with swaps on a seeded N(0,1) normalised 20-qubit state."""
+def test_qft20_parity(gpu):
+    """QFT with swaps on a seeded N(0,1) normalised 20-qubit state."""
     n = 20
     init = rng.normal_state(n, 1)
     ops = qft_with_swaps(n)

@@ -84,7 +84,7 @@ def test_measurement_28_qubits_shots_and_hamiltonian_match_oracle(gpu):
     assert abs(e_gpu - e_orc) <= 1e-12, (e_gpu, e_orc)
 
 
-def _config4():
+def _adjoint24():
     n, layers = 24, 8
     ops, pidx = adjoint.hardware_efficient_ansatz(n, layers)
     theta = (rng.uniforms(6, len(pidx)) * 2 - 1) * math.pi
@@ -95,7 +95,7 @@ def _config4():
 
 
 def test_adjoint_24_qubits_384_parameters(gpu):
-    n, ops, pidx, theta, H = _config4()
+    n, ops, pidx, theta, H = _adjoint24()
     assert len(pidx) == 384
     s = State(n)
     e, g = adjoint.adjoint_gradient(s, adjoint.set_params(ops, pidx, theta), pidx, H)

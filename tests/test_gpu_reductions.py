@@ -76,7 +76,7 @@ def test_pauli_sum_tile_path(gpu, n):
     assert abs(got - want) < 1e-12 * max(1.0, sum(abs(t[0]) for t in terms))
 
 
-def test_ising_hamiltonian_config3_form(gpu):
+def test_ising_hamiltonian_chain_form(gpu):
     n = 16
     re, im = rng.normal_state(n, 3)
     s = State.from_arrays(re, im)
