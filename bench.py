@@ -389,7 +389,8 @@ def gpu_arm(args) -> None:
     abytes = algorithmic_bytes(ops, n)
     N = 1 << n
     mode = nat.EXEC_DEFAULT if args.exact else nat.EXEC_FAST
-    mode |= {"threads": 0, "tma": nat.EXEC_TMA, "tma-prefetch": nat.EXEC_TMA_PREFETCH}[args.staging]
+    mode |= {"threads": 0, "tma": nat.EXEC_TMA, "tma-prefetch": nat.EXEC_TMA_PREFETCH,
+             "shuffle": nat.EXEC_SHUFFLE}[args.staging]
     re_t = torch.empty(N, dtype=torch.float64, device="cuda")
     im_t = torch.empty(N, dtype=torch.float64, device="cuda")
     state = State.from_torch(re_t, im_t)
@@ -605,6 +606,60 @@ def _event_time(fn, steps: int, warmup: int) -> float:
     e1.record()
     torch.cuda.synchronize()
     return e0.elapsed_time(e1) / 1e3 / steps
+
+
+def narrow_ops(n: int, layers: int, seed: int = 3):
+    """A circuit on qubits 0-4 of an n-qubit state: per layer U on each of the
+    five, then CX(0,1) CX(2,3) CX(1,2) CX(3,4)."""
+    from spinoza_gb300 import _native as nat
+    from spinoza_gb300 import rng
+
+    ang = rng.uniforms(seed, 15 * layers) * (2.0 * math.pi)
+    rows, k = [], 0
+    for _ in range(layers):
+        for q in range(5):
+            rows.append(((nat.U, 0, 0, 0, (ang[k], ang[k + 1], ang[k + 2])), q, nat.CONTROLS_NONE, 0, 0))
+            k += 3
+        for q in (0, 2, 1, 3):
+            rows.append(((nat.X, 0, 0, 0, (0.0, 0.0, 0.0)), q + 1, nat.CONTROLS_SINGLE, 1 << q, 0))
+    ops = np.zeros(len(rows), dtype=nat.OP_DTYPE)
+    for i, r in enumerate(rows):
+        ops[i] = r
+    return ops
+
+
+def workload_narrow(args) -> None:
+    """The narrow circuit (every gate on qubits 0-4; one fused pass) on an
+    n-qubit state, fast and exact mode, with the chosen tile staging: device
+    time of the pass, FP64 rate against the live DFMA probe."""
+    from spinoza_gb300 import _native as nat
+    from spinoza_gb300 import core
+    from spinoza_gb300.core import State
+
+    n, layers = args.qubits, args.layers
+    ops = narrow_ops(n, layers)
+    staging = {"threads": 0, "tma": nat.EXEC_TMA, "tma-prefetch": nat.EXEC_TMA_PREFETCH,
+               "shuffle": nat.EXEC_SHUFFLE}[args.staging]
+    s = State(n)
+    rate = core.fp64_fma_rate()
+    out = {}
+    for mode, base in (("fast", nat.EXEC_FAST), ("exact", nat.EXEC_DEFAULT)):
+        ms = []
+        for i in range(args.warmup + args.steps):
+            s.reset_zero()
+            tr, st = nat.spz_tracker(0, 0), nat.spz_exec_stats()
+            nat.check(nat.lib().spz_circuit_execute(s.handle, nat.ptr(ops), len(ops), nat.byref(tr),
+                                                    base | staging | nat.EXEC_TIME_PASSES, nat.byref(st)))
+            if i >= args.warmup:
+                ms.append(st.tile_ms + st.plain_ms)
+        t = sum(ms) / len(ms)
+        out[mode] = {"ms": t, "passes": int(st.passes), "tile_passes": int(st.tile_passes),
+                     "ops_in_shuffle_runs": int(st.shuffle_gates), "fp64_per_s": st.fp64_ops / (t / 1e3),
+                     "fp64_frac": st.fp64_ops / (t / 1e3) / rate, "gb_s": st.algorithmic_bytes / (t / 1e3) / 1e9}
+    _line(f"narrow circuit ({layers} layers on qubits 0-4) FP64 gate-apply GB/s", out["fast"]["gb_s"], "GB/s", args,
+          config={"workload": f"narrow-{n}q-{layers}layers (U on qubits 0-4, CX(0,1) CX(2,3) CX(1,2) CX(3,4) per "
+                              f"layer; from |0...0>)", "qubits": n, "layers": layers, "gates": len(ops)},
+          staging=args.staging, modes=out, dfma_rate=rate, higher_is_better=True)
 
 
 def workload_qft20(args) -> None:
@@ -853,7 +908,7 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="brickwork",
-                    choices=["brickwork", "qft20", "measure28", "batch", "sweep33", "gate"])
+                    choices=["brickwork", "qft20", "measure28", "batch", "sweep33", "gate", "narrow"])
     ap.add_argument("--gate", default="H", choices=["H", "X", "RX", "RY", "RZ", "U"], help="gate workload: kind")
     ap.add_argument("--target", type=int, default=5, help="gate workload: target qubit")
     ap.add_argument("--lazy", action="store_true", help="gate workload: the lazy per-gate mode")
@@ -882,8 +937,9 @@ def main() -> None:
     ap.add_argument("--no-parity", action="store_true")
     ap.add_argument("--no-sweep", action="store_true", help="skip the per-gate sweep at the headline's qubit count")
     ap.add_argument("--exact", action="store_true", help="time the bit-exact executor mode instead of fast mode")
-    ap.add_argument("--staging", default="threads", choices=["threads", "tma", "tma-prefetch"],
-                    help="how fused passes load their tiles: thread loads (default) or TMA gathers")
+    ap.add_argument("--staging", default="threads", choices=["threads", "tma", "tma-prefetch", "shuffle"],
+                    help="how fused passes stage their tiles: thread loads (default), TMA gathers, or "
+                         "thread loads with warp-shuffle runs for gates on the five lowest tile qubits")
     args = ap.parse_args()
     if args.impl == "reference":
         reference_arm(args)
@@ -894,7 +950,7 @@ def main() -> None:
 
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         {"qft20": workload_qft20, "measure28": workload_measure28, "batch": workload_batch,
-         "sweep33": workload_sweep33, "gate": workload_gate}[args.workload](args)
+         "sweep33": workload_sweep33, "gate": workload_gate, "narrow": workload_narrow}[args.workload](args)
 
 
 if __name__ == "__main__":

@@ -225,6 +225,10 @@ typedef struct spz_tracker {
                                     instead of thread loads; same results               */
 #define SPZ_EXEC_TMA_PREFETCH 64u /* as SPZ_EXEC_TMA, and the next tile is fetched while
                                     the current one computes (two tile buffers)          */
+#define SPZ_EXEC_SHUFFLE 128u    /* fused tile passes apply runs of gates on the five
+                                    lowest tile qubits with warp shuffles, amplitudes in
+                                    registers and no block barrier between the gates of
+                                    a run; same results                                 */
 
 /* Execution counters filled by spz_circuit_execute (may be NULL). */
 typedef struct spz_exec_stats {
@@ -236,6 +240,7 @@ typedef struct spz_exec_stats {
   uint64_t fp64_ops;       /* FP64-pipe instructions the gates' arithmetic needs    */
   double tile_ms;          /* SPZ_EXEC_TIME_PASSES: device time of the tile passes  */
   double plain_ms;         /* SPZ_EXEC_TIME_PASSES: device time of plain gate passes */
+  uint64_t shuffle_gates;  /* SPZ_EXEC_SHUFFLE: ops applied in warp-shuffle runs     */
 } spz_exec_stats;
 
 /* QuantumCircuit::execute (circuit.rs:552-600): apply `ops` in order.

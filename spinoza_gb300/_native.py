@@ -39,6 +39,7 @@ EXEC_FAST = 8
 BATCH_WIDE_APART = 16
 EXEC_TMA = 32
 EXEC_TMA_PREFETCH = 64
+EXEC_SHUFFLE = 128
 MAX_QUBITS = 34
 
 
@@ -74,7 +75,7 @@ class spz_tracker(ctypes.Structure):
 class spz_exec_stats(ctypes.Structure):
     _fields_ = [("gates", c_uint64), ("passes", c_uint64), ("tile_passes", c_uint64),
                 ("bytes_moved", c_uint64), ("algorithmic_bytes", c_uint64), ("fp64_ops", c_uint64),
-                ("tile_ms", c_double), ("plain_ms", c_double)]
+                ("tile_ms", c_double), ("plain_ms", c_double), ("shuffle_gates", c_uint64)]
 
 
 class spz_pauli_term(ctypes.Structure):

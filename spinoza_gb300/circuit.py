@@ -349,13 +349,15 @@ class Program:
     """A circuit planned once and replayed as a CUDA graph (spz_program_*):
     ``Program(n, ops).run(state)`` applies `ops` to an n-qubit state with no
     planning or uploads per run.  No measurements; fused / fast as in
-    QuantumCircuit.  Runs are asynchronous on the state's stream."""
+    QuantumCircuit.  Runs are asynchronous on the state's stream.
+    `extra_flags` adds executor flags (EXEC_SHUFFLE)."""
 
-    def __init__(self, n: int, ops: np.ndarray, fused: bool = True, fast: bool = False):
+    def __init__(self, n: int, ops: np.ndarray, fused: bool = True, fast: bool = False, extra_flags: int = 0):
         self.n = int(n)
         ops = np.ascontiguousarray(ops, dtype=nat.OP_DTYPE)
         h = nat.c_void_p()
-        nat.check(nat.lib().spz_program_create(self.n, nat.ptr(ops), len(ops), _flags(fused, fast), byref(h)))
+        flags = _flags(fused, fast) | int(extra_flags)
+        nat.check(nat.lib().spz_program_create(self.n, nat.ptr(ops), len(ops), flags, byref(h)))
         self._h = h
 
     def run(self, state: State) -> None:

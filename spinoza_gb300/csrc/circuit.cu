@@ -190,12 +190,232 @@ __device__ __forceinline__ void tile_phase_pm(const TileGate& g, const double2* 
   }
 }
 
+// ------------------------------------------------ warp-shuffle runs
+// SPZ_EXEC_SHUFFLE: a run of consecutive gates whose pairs lie inside 32
+// consecutive amplitudes of the tile (target on tile bits 0-4) is applied
+// with the amplitudes in registers: lane l of a warp holds amplitude 32 r + l
+// of rows r, the partner of a pair is fetched with __shfl_xor_sync, and no
+// block barrier separates the gates of the run (each warp owns its rows).
+// Each lane computes only its own member's outputs; every product that the
+// other member's output needs is computed by the lane that owns its operand
+// and passed across, so a pair costs the same FP64 instructions as in shared
+// memory and each result is formed by the same operations in the same order
+// (bit-identical to the shared-memory ops).  Eligible (chosen on the host):
+// X and Y with any controls, uncontrolled H / RX / RY and the fast-mode lazy
+// ops (with their phase entry), phase ops over the whole tile, and diagonal
+// gates whose every amplitude is touched (Z with any controls).
+__device__ __forceinline__ double shfl_x(double v, uint32_t m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+
+__device__ __forceinline__ uint32_t phase_index(const TileGate& g, uint64_t base, uint32_t e) {
+  uint32_t idx = 0;
+  for (int j = 0; j < g.pm; ++j)
+    idx |= (uint32_t)((__popcll(base & g.pmask[j]) ^ __popc(e & g.pemask[j])) & 1) << j;
+  return idx;
+}
+
+// Lazy op of a run: the descriptor's phase masks are read once per row group
+// into registers (PM of them; the table index of an amplitude is the tile's
+// parities xor the local ones).
+template <int R, int PM>
+__device__ __forceinline__ void run_lazy(const TileGate& g, const double2* __restrict__ tables, uint64_t base,
+                                         uint32_t lane, const uint32_t* e, double* xr, double* xi) {
+  const uint32_t tb = g.tbit;
+  const bool hi = (lane & tb) != 0;
+  const int kind = g.kind;
+  const double t = g.c.cs;
+  const double2* tab = tables + g.ptab;
+  uint32_t em[PM > 0 ? PM : 1];
+  uint32_t bidx = 0;
+#pragma unroll
+  for (int j = 0; j < PM; ++j) {
+    if (j < g.pm) {
+      bidx |= (uint32_t)(__popcll(base & g.pmask[j]) & 1) << j;
+      em[j] = g.pemask[j];
+    } else {
+      em[j] = 0;
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < R; ++u) {
+    double pr = shfl_x(xr[u], tb), pi = shfl_x(xi[u], tb);
+    if constexpr (PM > 0) {  // s1 x w: the s1 lane forms the real part, the s0 lane the imaginary part
+      uint32_t idx = bidx;
+#pragma unroll
+      for (int j = 0; j < PM; ++j) idx ^= (uint32_t)(__popc(e[u] & em[j]) & 1) << j;
+      const double2 w = __ldg(tab + idx);
+      const double r = hi ? xr[u] : pr, i = hi ? xi[u] : pi;
+      const double v = dfma(r, hi ? w.x : w.y, dmul(hi ? dneg(i) : i, hi ? w.y : w.x));
+      const double vp = shfl_x(v, tb);
+      if (hi) {
+        xr[u] = v; xi[u] = vp;
+      } else {
+        pr = vp; pi = v;
+      }
+    }
+    const double a = xr[u], b = xi[u];
+    switch (kind) {
+      case FK_LAZY_H: {  // s0 + s1, s0 - s1
+        const double sg = hi ? -1.0 : 1.0;
+        xr[u] = dfma(sg, a, pr); xi[u] = dfma(sg, b, pi);
+        break;
+      }
+      case FK_LAZY_RX_A:  // s0 - i t s1, -i t s0 + s1
+        xr[u] = dfma(t, pi, a); xi[u] = dfma(dneg(t), pr, b);
+        break;
+      case FK_LAZY_RX_B:  // u s0 - i s1, -i s0 + u s1
+        xr[u] = dfma(t, a, pi); xi[u] = dfma(t, b, dneg(pr));
+        break;
+      case FK_LAZY_RY_A: {  // s0 - t s1, t s0 + s1
+        const double ts = hi ? t : dneg(t);
+        xr[u] = dfma(ts, pr, a); xi[u] = dfma(ts, pi, b);
+        break;
+      }
+      default:  // FK_LAZY_RY_B: u s0 - s1, s0 + u s1
+        xr[u] = dfma(t, a, hi ? pr : dneg(pr)); xi[u] = dfma(t, b, hi ? pi : dneg(pi));
+    }
+  }
+}
+
+template <int R>
+__device__ __forceinline__ void run_pair(const TileGate& g, const double2* __restrict__ tables, uint64_t base,
+                                         uint32_t lane, const uint32_t* e, double* xr, double* xi) {
+  const uint32_t tb = g.tbit;
+  const bool hi = (lane & tb) != 0;
+  const int kind = g.kind;
+  if (kind == SPZ_GATE_X || kind == SPZ_GATE_Y) {
+#pragma unroll
+    for (int u = 0; u < R; ++u) {
+      const double pr = shfl_x(xr[u], tb), pi = shfl_x(xi[u], tb);
+      if (((e[u] & ~tb) & g.e_mask) == g.l_ones) {
+        if (kind == SPZ_GATE_X) {
+          xr[u] = pr; xi[u] = pi;
+        } else {  // (a, b, c, d) -> (d, -c, -b, a)
+          xr[u] = hi ? dneg(pi) : pi;
+          xi[u] = hi ? pr : dneg(pr);
+        }
+      }
+    }
+  } else if (kind == SPZ_GATE_H) {  // a' = a1 + c1, c' = a1 - c1 with x1 = x / sqrt 2
+    const double sg = hi ? -1.0 : 1.0;
+#pragma unroll
+    for (int u = 0; u < R; ++u) {
+      const double orr = dmul(kSqrtOneHalf, xr[u]), oi = dmul(kSqrtOneHalf, xi[u]);
+      const double qr = shfl_x(orr, tb), qi = shfl_x(oi, tb);
+      xr[u] = dfma(sg, orr, qr);
+      xi[u] = dfma(sg, oi, qi);
+    }
+  } else if (kind == SPZ_GATE_RY) {  // a' = a cos - c sin, c' = a sin + c cos
+    const double sg = hi ? 1.0 : -1.0, cs = g.c.cs, sn = g.c.sn;
+#pragma unroll
+    for (int u = 0; u < R; ++u) {
+      const double pr = dmul(xr[u], cs), pi = dmul(xi[u], cs);
+      const double qr = shfl_x(dmul(xr[u], sn), tb), qi = shfl_x(dmul(xi[u], sn), tb);
+      xr[u] = dfma(sg, qr, pr);
+      xi[u] = dfma(sg, qi, pi);
+    }
+  } else if (kind == SPZ_GATE_RX) {
+    // a' = a cos - d nsn, b' = b cos + c nsn, c' = b sn + c cos, d' = d cos + a nsn
+    const double sg = hi ? 1.0 : -1.0, cs = g.c.cs, nsn = g.c.nsn, sx = hi ? g.c.nsn : g.c.sn;
+#pragma unroll
+    for (int u = 0; u < R; ++u) {
+      const double pr = dmul(xr[u], cs), pi = dmul(xi[u], cs);
+      const double sp = shfl_x(dmul(xi[u], sx), tb), tp = shfl_x(dmul(xr[u], nsn), tb);
+      xr[u] = dfma(sg, sp, pr);
+      xi[u] = dfma(1.0, pi, tp);
+    }
+  } else {  // fast-mode lazy ops, s1 first multiplied by its phase entry when the op carries one
+    switch (g.pm) {
+      case 0: run_lazy<R, 0>(g, tables, base, lane, e, xr, xi); break;
+      case 1: run_lazy<R, 1>(g, tables, base, lane, e, xr, xi); break;
+      case 2: run_lazy<R, 2>(g, tables, base, lane, e, xr, xi); break;
+      case 3: run_lazy<R, 3>(g, tables, base, lane, e, xr, xi); break;
+      case 4: run_lazy<R, 4>(g, tables, base, lane, e, xr, xi); break;
+      default: run_lazy<R, kPhaseMaxTerms>(g, tables, base, lane, e, xr, xi); break;
+    }
+  }
+}
+
+template <int R>
+__device__ __forceinline__ void run_elementwise(const TileGate& g, const double2* __restrict__ tables, uint64_t base,
+                                                const uint32_t* e, double* xr, double* xi) {
+  if (g.mode == TM_PHASE) {  // the whole tile (a local half bit is never in a run)
+    const double2* tab = tables + g.ptab;
+#pragma unroll
+    for (int u = 0; u < R; ++u) {
+      const double2 w = __ldg(tab + phase_index(g, base, e[u]));
+      const double r = xr[u], i = xi[u];
+      xr[u] = dfma(r, w.x, dmul(dneg(i), w.y));
+      xi[u] = dfma(r, w.y, dmul(i, w.x));
+    }
+    return;
+  }
+  int gone = -1;
+  if (g.mode == TM_DIAG_GLOBAL) {
+    gone = (base & g.g_tbit) ? 1 : 0;
+    if (!gone && g.kind != SPZ_GATE_RZ) return;  // Z / P act on the 1 half only
+  }
+#pragma unroll
+  for (int u = 0; u < R; ++u) {
+    if ((e[u] & g.e_mask) != g.l_ones) continue;
+    const bool one = gone >= 0 ? gone != 0 : (e[u] & g.tbit) != 0;
+    switch (g.kind) {
+      case SPZ_GATE_Z: gate_diag<SPZ_GATE_Z>(g.c, one, xr[u], xi[u]); break;
+      case SPZ_GATE_P: gate_diag<SPZ_GATE_P>(g.c, one, xr[u], xi[u]); break;
+      default: gate_diag<SPZ_GATE_RZ>(g.c, one, xr[u], xi[u]); break;
+    }
+  }
+}
+
+// Gates g0 .. g1 - 1 of the pass as one run; rows of 32 amplitudes, R per
+// warp at a time.  Requires 2^k >= 32 R and whole warps.
+constexpr int kRunRows = 4;
+
+__device__ void tile_run_shfl(const PassArgs& A, uint64_t base, double* sre, double* sim, uint32_t T, int g0,
+                              int g1) {
+  constexpr int R = kRunRows;
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  const uint32_t rows = T >> 5;
+  for (uint32_t r0 = warp * R; r0 < rows; r0 += nwarps * R) {
+    uint32_t e[R];
+    double xr[R], xi[R];
+#pragma unroll
+    for (int u = 0; u < R; ++u) {
+      e[u] = ((r0 + u) << 5) | lane;
+      xr[u] = sre[TileSwizzle::at(e[u])];
+      xi[u] = sim[TileSwizzle::at(e[u])];
+    }
+    for (int gi = g0; gi < g1; ++gi) {
+      const TileGate& g = A.gates[gi];
+      if ((base & g.g_ones) != g.g_ones || (base & g.g_zeros) != 0) continue;
+      if (g.cond >= 0 && A.outcomes[g.cond] == 0) continue;
+      if (g.mode == TM_PAIR) run_pair<R>(g, A.tables, base, lane, e, xr, xi);
+      else run_elementwise<R>(g, A.tables, base, e, xr, xi);
+    }
+#pragma unroll
+    for (int u = 0; u < R; ++u) {
+      sre[TileSwizzle::at(e[u])] = xr[u];
+      sim[TileSwizzle::at(e[u])] = xi[u];
+    }
+  }
+}
+
 // Every gate of the pass on one tile held in shared memory (sre, sim), in
-// pass order, with a block barrier after each.
+// pass order, with a block barrier after each (with SHFL, after each run of
+// warp-shuffle gates; without, runs are ignored and every gate is applied in
+// shared memory).
+template <bool SHFL>
 __device__ __forceinline__ void tile_pass_gates(const PassArgs& A, uint64_t base, double* sre, double* sim,
                                                 uint32_t T) {
   for (int gi = 0; gi < A.ngates; ++gi) {
     const TileGate& g = A.gates[gi];
+    if constexpr (SHFL) {
+      if (g.run_end > gi) {
+        tile_run_shfl(A, base, sre, sim, T, gi, g.run_end);
+        gi = g.run_end - 1;
+        __syncthreads();
+        continue;
+      }
+    }
     if ((base & g.g_ones) != g.g_ones || (base & g.g_zeros) != 0) continue;  // uniform per tile
     if (g.cond >= 0 && A.outcomes[g.cond] == 0) continue;                   // classical condition
     const uint32_t nw = T >> g.npos;
@@ -246,6 +466,7 @@ __device__ __forceinline__ void tile_pass_gates(const PassArgs& A, uint64_t base
   }
 }
 
+template <bool SHFL>
 __global__ void __launch_bounds__(kTileThreads, SPZ_TILE_MIN_BLOCKS) tile_kernel(PassArgs A) {
   extern __shared__ double smem[];
   const int K = A.k;
@@ -287,7 +508,7 @@ __global__ void __launch_bounds__(kTileThreads, SPZ_TILE_MIN_BLOCKS) tile_kernel
       *reinterpret_cast<double2*>(sim + p) = m;
     }
     __syncthreads();
-    tile_pass_gates(A, base, sre, sim, T);
+    tile_pass_gates<SHFL>(A, base, sre, sim, T);
     // store
     for (uint32_t e2 = threadIdx.x; e2 < T / 2; e2 += blockDim.x) {
       const uint32_t e = 2 * e2;
@@ -431,7 +652,7 @@ __global__ void __launch_bounds__(kTileThreads) tile_kernel_tma(PassArgs A, cons
     double* sre = bufs + (size_t)b * 2 * T;
     double* sim = sre + T;
     const uint64_t base = deposit(tile, A.lpos, K);
-    tile_pass_gates(A, base, sre, sim, T);
+    tile_pass_gates<false>(A, base, sre, sim, T);
     for (uint32_t e2 = threadIdx.x; e2 < T / 2; e2 += blockDim.x) {  // store, as the thread-load kernel
       const uint32_t e = 2 * e2;
       const uint64_t gi = base | rowoff[e >> kTileLowBits] | (e & ((1u << kTileLowBits) - 1));
@@ -576,6 +797,7 @@ TileGate tile_gate(const GateApp& g, const std::vector<int>& local, const std::v
         t.g_ones = tab.half_bit;
       }
     }
+    t.e_mask = t.l_ones;
     return t;
   }
   uint32_t l_ones = 0, l_zeros = 0;
@@ -627,6 +849,7 @@ TileGate tile_gate(const GateApp& g, const std::vector<int>& local, const std::v
   t.npos = 0;
   for (int j = 0; j < 32; ++j)
     if ((special >> j) & 1) t.pos[t.npos++] = (uint8_t)j;
+  t.e_mask = special;
   return t;
 }
 
@@ -634,6 +857,58 @@ TileGate tile_gate(const GateApp& g, const std::vector<int>& local, const std::v
 }  // namespace
 
 TileGate make_tile_gate(const GateApp& g, const std::vector<int>& local) { return tile_gate(g, local); }
+
+namespace {
+
+// Gates that tile_run_shfl applies: pairs inside a row of 32 amplitudes whose
+// per-lane split costs no extra FP64 work, and elementwise ops that touch
+// every amplitude of the tile (Z, with no FP64 work, under any controls).
+bool shfl_eligible(const TileGate& t) {
+  switch (t.mode) {
+    case TM_PAIR:
+      if (t.tbit >= 32u) return false;
+      if (t.kind == SPZ_GATE_X || t.kind == SPZ_GATE_Y) return true;
+      if (t.kind == SPZ_GATE_H || t.kind == SPZ_GATE_RX || t.kind == SPZ_GATE_RY ||
+          (t.kind >= FK_LAZY_H && t.kind <= FK_LAZY_RY_B))
+        return t.e_mask == t.tbit;  // uncontrolled within the tile
+      return false;
+    case TM_PHASE:
+      return t.npos == 0;
+    case TM_DIAG_LOCAL:
+    case TM_DIAG_GLOBAL:
+      return t.kind == SPZ_GATE_Z || t.e_mask == 0;
+    default:
+      return false;
+  }
+}
+
+// A run shorter than this gains nothing over the shared-memory ops (its rows
+// are loaded and stored once either way).
+constexpr int kMinShuffleRun = 2;
+
+// SPZ_EXEC_SHUFFLE: mark the runs in one tile pass's descriptors g[0 .. count)
+// (a pass of k local qubits: rows of 32 amplitudes, kRunRows per warp).
+// Returns the number of gates in runs.
+size_t mark_shuffle_runs(TileGate* g, size_t count, int k) {
+  if ((1u << k) < 32u * kRunRows) return 0;
+  size_t in_runs = 0;
+  for (size_t i = 0; i < count;) {
+    if (!shfl_eligible(g[i])) {
+      ++i;
+      continue;
+    }
+    size_t j = i + 1;
+    while (j < count && shfl_eligible(g[j])) ++j;
+    if (j - i >= (size_t)kMinShuffleRun) {
+      g[i].run_end = (int32_t)j;
+      in_runs += j - i;
+    }
+    i = j;
+  }
+  return in_runs;
+}
+
+}  // namespace
 
 namespace {
 
@@ -680,6 +955,24 @@ struct PassTimer {
 
 }  // namespace
 
+// A tile pass whose gates touch fewer than k qubits gets the lowest untouched
+// qubits as extra local qubits: its tiles then hold 2^k amplitudes, so every
+// thread of a block has pairs to work on (a pass on 5 qubits would otherwise
+// run 32-amplitude tiles with half of each warp idle in every pair op).  The
+// tiling is only a partition of the amplitudes: results are unchanged.
+static void pad_tile_passes(std::vector<PlannedPass>& passes, uint32_t n, int k) {
+  for (PlannedPass& P : passes) {
+    const bool tiled = P.gates.size() > 1 || P.gates[0].kind >= FK_LAZY_H || P.gates[0].cond >= 0;
+    if (!tiled || (int)P.local.size() >= k) continue;
+    uint64_t L = 0;
+    for (int q : P.local) L |= 1ull << q;
+    for (int q = 0; q < (int)n && __builtin_popcountll(L) < k; ++q) L |= 1ull << q;
+    P.local.clear();
+    for (int q = 0; q < (int)n; ++q)
+      if ((L >> q) & 1) P.local.push_back(q);
+  }
+}
+
 std::vector<PlannedPass> plan_passes(const std::vector<GateApp>& gates, uint32_t n, int k, int c, bool exact) {
   return plan(gates, n, k, c, exact);
 }
@@ -702,27 +995,31 @@ uint64_t op_fp64_ops(uint32_t n, const GateApp& g, const std::vector<PhaseTable>
 // count; the grid of a tile pass is one wave of them (each block loops over
 // tiles), so no block waits for a second wave.  Cached per device and tile
 // size (kernel attributes are per device); callers may be on several threads.
-int tile_launch_shape(int device, int threads, size_t smem, int* resident_out, int* sms_out) {
+int tile_launch_shape(int device, int threads, size_t smem, int* resident_out, int* sms_out, bool shfl) {
   static std::mutex mu;
   static int sms[kMaxDevices] = {};
-  static int resident[kMaxDevices][kTileMaxK + 2][2] = {};  // by log2 of the tile, and 32 / 64 threads
+  // by log2 of the tile, 32 / 64 threads, and the instantiation
+  static int resident[kMaxDevices][kTileMaxK + 2][2][2] = {};
   if (device < 0 || device >= kMaxDevices) return fail(SPZ_ERR_INVALID_ARGUMENT, "device index out of range");
   std::lock_guard<std::mutex> lock(mu);
   if (!sms[device]) {
     int count = 0;
     SPZ_CUDA(cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount, device));
     const int max_smem = (2 << kTileMaxK) * 8 + (1 << (kTileMaxK - kTileLowBits)) * 8;
-    SPZ_CUDA(cudaFuncSetAttribute(tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
-    SPZ_CUDA(cudaFuncSetAttribute(tile_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                  cudaSharedmemCarveoutMaxShared));
+    for (const void* fn : {(const void*)tile_kernel<false>, (const void*)tile_kernel<true>}) {
+      SPZ_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, max_smem));
+      SPZ_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                    cudaSharedmemCarveoutMaxShared));
+    }
     sms[device] = count;
   }
   int lg = 0;  // the largest lg with 2 x 8 B x 2^lg <= smem (the tile's re and im)
   while (lg <= kTileMaxK && (16ull << (lg + 1)) <= smem) ++lg;
-  int& r = resident[device][lg][threads > 32 ? 1 : 0];
+  int& r = resident[device][lg][threads > 32 ? 1 : 0][shfl ? 1 : 0];
   if (!r) {
     int per_sm = 0;
-    SPZ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tile_kernel, threads, smem));
+    const void* fn = shfl ? (const void*)tile_kernel<true> : (const void*)tile_kernel<false>;
+    SPZ_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, threads, smem));
     r = std::max(1, per_sm);
   }
   *resident_out = r;
@@ -927,6 +1224,7 @@ int run_gates_io(spz_state_t h, const std::vector<GateApp>& gates_in, uint32_t f
   const int k = std::min<int>((int)n, h->tile_k ? h->tile_k : kTileMaxK);
   const int c = std::min<int>(kTileLowBits, k);
   std::vector<PlannedPass> passes = plan(gates, n, k, c, !fast);
+  pad_tile_passes(passes, n, k);
   // Phase tables, flattened (re, im) after the gate list.
   std::vector<uint32_t> table_offsets;
   std::vector<double> flat;
@@ -946,8 +1244,13 @@ int run_gates_io(spz_state_t h, const std::vector<GateApp>& gates_in, uint32_t f
   std::vector<size_t> offs;
   for (const PlannedPass& P : passes) {
     offs.push_back(all.size());
-    if (tiled(P))
+    if (tiled(P)) {
       for (const GateApp& g : P.gates) all.push_back(tile_gate(g, P.local, &tables, &table_offsets));
+      if (flags & SPZ_EXEC_SHUFFLE) {
+        const size_t r = mark_shuffle_runs(all.data() + offs.back(), P.gates.size(), (int)P.local.size());
+        if (st) st->shuffle_gates += r;
+      }
+    }
   }
   TileGate* dgates = nullptr;
   const double2* dtables = nullptr;
@@ -968,6 +1271,7 @@ int run_gates_io(spz_state_t h, const std::vector<GateApp>& gates_in, uint32_t f
 
   // TMA staging (SPZ_EXEC_TMA*): tensor maps once per handle; the timeout word
   // is cleared here and read back at the end of the run.
+  const bool shfl = (flags & SPZ_EXEC_SHUFFLE) != 0;
   bool use_tma = false;
 #if !SPZ_TILE_SWIZZLE
   if ((flags & (SPZ_EXEC_TMA | SPZ_EXEC_TMA_PREFETCH)) && n >= 5) {
@@ -1010,7 +1314,7 @@ int run_gates_io(spz_state_t h, const std::vector<GateApp>& gates_in, uint32_t f
     const int threads = h->tile_threads ? h->tile_threads
                                         : (int)std::min<uint32_t>(kTileThreads, std::max<uint32_t>(32, T / 2));
     int resident = 0, sms = 0;
-    int rc = tile_launch_shape(h->device, threads, smem, &resident, &sms);
+    int rc = tile_launch_shape(h->device, threads, smem, &resident, &sms, shfl);
     if (rc) return rc;
     if (use_tma && A.c == kTileLowBits && A.k >= kTileLowBits + 2) {
       const bool pre = (flags & SPZ_EXEC_TMA_PREFETCH) != 0;
@@ -1028,7 +1332,8 @@ int run_gates_io(spz_state_t h, const std::vector<GateApp>& gates_in, uint32_t f
       return SPZ_OK;
     }
     const uint64_t blocks = std::min<uint64_t>(per, (uint64_t)sms * resident);
-    tile_kernel<<<(unsigned)blocks, threads, smem, h->stream>>>(A);
+    if (shfl) tile_kernel<true><<<(unsigned)blocks, threads, smem, h->stream>>>(A);
+    else tile_kernel<false><<<(unsigned)blocks, threads, smem, h->stream>>>(A);
     SPZ_CHECK_LAUNCH("tile_kernel");
     return SPZ_OK;
   };
@@ -1327,7 +1632,15 @@ int plan_stats(uint32_t n, const spz_op* ops, size_t nops, uint32_t flags, spz_e
     } else {
       const int k = std::min<int>((int)n, kTileMaxK);
       const int c = std::min<int>(kTileLowBits, k);
-      for (const PlannedPass& P : plan(run, n, k, c, !fast)) {
+      const std::vector<uint32_t> no_offsets(tables.size(), 0);
+      std::vector<PlannedPass> planned = plan(run, n, k, c, !fast);
+      pad_tile_passes(planned, n, k);
+      for (const PlannedPass& P : planned) {
+        if ((flags & SPZ_EXEC_SHUFFLE) && (P.gates.size() > 1 || P.gates[0].kind >= FK_LAZY_H || P.gates[0].cond >= 0)) {
+          std::vector<TileGate> tg;
+          for (const GateApp& g : P.gates) tg.push_back(tile_gate(g, P.local, &tables, &no_offsets));
+          st->shuffle_gates += mark_shuffle_runs(tg.data(), tg.size(), (int)P.local.size());
+        }
         if (order && !fast)
           for (const GateApp& g : P.gates) {
             order->push_back((uint32_t)g.src);
@@ -1389,6 +1702,7 @@ struct ProgramPass {
   int threads = 0;
   size_t smem = 0;
   uint64_t blocks = 0;
+  bool shfl = false;   // tiled: launched as tile_kernel<true> (SPZ_EXEC_SHUFFLE)
 };
 
 }  // namespace spz
@@ -1455,6 +1769,7 @@ int build_program(spz_program_t p, const spz_op* ops, size_t nops, uint32_t flag
   const int k = std::min<int>((int)n, kTileMaxK);
   const int c = std::min<int>(kTileLowBits, k);
   std::vector<PlannedPass> planned = plan(gates, n, k, c, !fast);
+  pad_tile_passes(planned, n, k);
   std::vector<uint32_t> table_offsets;
   std::vector<double> flat;
   for (const PhaseTable& t : tables) {
@@ -1469,8 +1784,11 @@ int build_program(spz_program_t p, const spz_op* ops, size_t nops, uint32_t flag
   for (const PlannedPass& P : planned) {
     offs.push_back(all.size());
     const bool tiled = P.gates.size() > 1 || P.gates[0].kind >= FK_LAZY_H || P.gates[0].cond >= 0;
-    if (tiled)
+    if (tiled) {
       for (const GateApp& g : P.gates) all.push_back(tile_gate(g, P.local, &tables, &table_offsets));
+      if (flags & SPZ_EXEC_SHUFFLE)
+        p->stats.shuffle_gates += mark_shuffle_runs(all.data() + offs.back(), P.gates.size(), (int)P.local.size());
+    }
   }
   const size_t gbytes = (all.size() * sizeof(TileGate) + 255) / 256 * 256;
   const size_t tbytes = flat.size() * sizeof(double);
@@ -1504,8 +1822,9 @@ int build_program(spz_program_t p, const spz_op* ops, size_t nops, uint32_t flag
     const uint32_t T = 1u << A.k;
     pp.smem = 2 * T * sizeof(double) + (size_t)(1u << A.nhigh) * sizeof(uint64_t);
     pp.threads = (int)std::min<uint32_t>(kTileThreads, std::max<uint32_t>(32, T / 2));
+    pp.shfl = (flags & SPZ_EXEC_SHUFFLE) != 0;
     int resident = 0, sms = 0;
-    int rc = tile_launch_shape(p->device, pp.threads, pp.smem, &resident, &sms);
+    int rc = tile_launch_shape(p->device, pp.threads, pp.smem, &resident, &sms, pp.shfl);
     if (rc) return rc;
     pp.blocks = std::min<uint64_t>(A.ntiles, (uint64_t)sms * resident);
     p->stats.tile_passes++;
@@ -1536,7 +1855,8 @@ int capture_program(spz_program_t p, spz_state_t h) {
       A.re = h->re;
       A.im = h->im;
       A.outcomes = nullptr;
-      tile_kernel<<<(unsigned)pp.blocks, pp.threads, pp.smem, p->capture>>>(A);
+      if (pp.shfl) tile_kernel<true><<<(unsigned)pp.blocks, pp.threads, pp.smem, p->capture>>>(A);
+      else tile_kernel<false><<<(unsigned)pp.blocks, pp.threads, pp.smem, p->capture>>>(A);
       cudaError_t le = cudaGetLastError();
       if (le != cudaSuccess) rc = cuda_fail(le, "tile_kernel");
     }

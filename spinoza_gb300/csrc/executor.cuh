@@ -48,6 +48,10 @@ struct TileGate {
   int32_t pm;
   uint32_t ptab;
   int32_t cond;  // >= 0: applies only if that qubit's device-side measurement read 1
+  uint32_t e_mask;  // pos[0 .. npos - 1] as a bit mask of the tile offset
+  // SPZ_EXEC_SHUFFLE: > this gate's index, the end of a run of gates that the
+  // block applies with warp shuffles (circuit.cu, tile_run_shfl); 0 otherwise.
+  int32_t run_end;
 };
 
 // The descriptor of gate g inside a tile pass whose local qubits are `local`

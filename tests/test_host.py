@@ -41,7 +41,7 @@ def test_struct_layouts():
     assert ctypes.sizeof(nat.spz_gate) == 40
     assert ctypes.sizeof(nat.spz_op) == 64
     assert ctypes.sizeof(nat.spz_pauli_term) == 24
-    assert ctypes.sizeof(nat.spz_exec_stats) == 64
+    assert ctypes.sizeof(nat.spz_exec_stats) == 72
 
 
 def test_rng_stream_matches_oracle():
@@ -119,6 +119,29 @@ def test_planner_fuses_brickwork(native):
     assert st["passes"] < st["gates"] / 4, st
     # the algorithmic bytes are the unfused minimum
     assert st["algorithmic_bytes"] == layers * (n * 32 + (n - 1) * 16) << n
+
+
+def test_planner_marks_shuffle_runs(native):
+    """SPZ_EXEC_SHUFFLE: runs of at least two consecutive ops on the five lowest
+    tile qubits are marked (fast brickwork: the lazy rotations and CX there);
+    none without the flag, none in tiles of fewer than 2^7 amplitudes."""
+    n = 30
+    ops = brickwork_ops(n, 4)
+    counts = {}
+    for flags in (nat.EXEC_FAST, nat.EXEC_FAST | nat.EXEC_SHUFFLE, nat.EXEC_SHUFFLE):
+        st = nat.spz_exec_stats()
+        nat.check(nat.lib().spz_plan_stats(n, nat.ptr(ops), len(ops), flags, nat.byref(st)))
+        counts[flags] = (st.shuffle_gates, st.passes)
+    assert counts[nat.EXEC_FAST][0] == 0
+    assert counts[nat.EXEC_FAST | nat.EXEC_SHUFFLE][0] > 0
+    assert counts[nat.EXEC_FAST | nat.EXEC_SHUFFLE][1] == counts[nat.EXEC_FAST][1]  # same passes
+    # exact U is not run-eligible (its pair arithmetic does not split evenly over two lanes); CX is
+    assert counts[nat.EXEC_SHUFFLE][0] > 0
+    small = brickwork_ops(6, 4)
+    st = nat.spz_exec_stats()
+    nat.check(nat.lib().spz_plan_stats(6, nat.ptr(small), len(small), nat.EXEC_FAST | nat.EXEC_SHUFFLE,
+                                       nat.byref(st)))
+    assert st.shuffle_gates == 0
 
 
 def random_ops(n, ngates, seed):
