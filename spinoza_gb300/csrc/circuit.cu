@@ -18,6 +18,8 @@
 #include <cudaTypedefs.h>
 
 #include <algorithm>
+#include <complex>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -187,6 +189,79 @@ __device__ __forceinline__ void tile_phase_pm(const TileGate& g, const double2* 
     case 6: tile_phase<NPOS, 6>(g, tab, base, sre, sim, nelem); break;
     case 7: tile_phase<NPOS, 7>(g, tab, base, sre, sim, nelem); break;
     default: tile_phase<NPOS, kPhaseMaxTerms>(g, tab, base, sre, sim, nelem); break;
+  }
+}
+
+// Fast mode, two lazy rotations fused (TM_LAZY2): on each block of four
+// amplitudes (tile bits b1 = tbit, b2 = tbit2), the first op's phase on the
+// b1 = 1 half and the second op's phase on the b2 = 1 half are applied
+// together (the second op's phase masks never contain the first op's qubit,
+// so it commutes with the first rotation): three complex multiplies by one
+// table row instead of four, then the first rotation on the two pairs along
+// b1 and the second on the two pairs along b2.  28 FP64 instructions per
+// block instead of 32, one shared-memory round trip and one barrier for both.
+template <int PM>
+__device__ __forceinline__ void tile_lazy2(const TileGate& g, const double2* __restrict__ tab, uint64_t base,
+                                           double* sre, double* sim, uint32_t nblocks) {
+  const Enumerator<2, TileGate> E(g);
+  const uint32_t b1 = g.tbit, b2 = g.tbit2;
+  const double t1 = g.c.cs, t2 = g.c.sn;
+  const int k1 = g.kind, k2 = g.kind2;
+  uint32_t em[PM > 0 ? PM : 1];
+  uint32_t bidx = 0;
+#pragma unroll
+  for (int j = 0; j < PM; ++j) {
+    if (j < g.pm) {
+      bidx |= (uint32_t)(__popcll(base & g.pmask[j]) & 1) << j;
+      em[j] = g.pemask[j];
+    } else {
+      em[j] = 0;
+    }
+  }
+  for (uint32_t m = threadIdx.x; m < nblocks; m += blockDim.x) {
+    const uint32_t e = E(m);
+    uint32_t idx = bidx;
+#pragma unroll
+    for (int j = 0; j < PM; ++j) idx ^= (uint32_t)(__popc(e & em[j]) & 1) << j;
+    const double2* row = tab + 3 * idx;
+    const uint32_t e1 = TileSwizzle::at(e | b1), e2 = TileSwizzle::at(e | b2), e3 = TileSwizzle::at(e | b1 | b2);
+    const uint32_t e0 = TileSwizzle::at(e);
+    double r0 = sre[e0], i0 = sim[e0];
+    double r1 = sre[e1], i1 = sim[e1];
+    double r2 = sre[e2], i2 = sim[e2];
+    double r3 = sre[e3], i3 = sim[e3];
+    {
+      const double2 w1 = __ldg(row), w2 = __ldg(row + 1), w3 = __ldg(row + 2);
+      double x = r1, y = i1;
+      r1 = dfma(x, w1.x, dmul(dneg(y), w1.y));
+      i1 = dfma(x, w1.y, dmul(y, w1.x));
+      x = r2; y = i2;
+      r2 = dfma(x, w2.x, dmul(dneg(y), w2.y));
+      i2 = dfma(x, w2.y, dmul(y, w2.x));
+      x = r3; y = i3;
+      r3 = dfma(x, w3.x, dmul(dneg(y), w3.y));
+      i3 = dfma(x, w3.y, dmul(y, w3.x));
+    }
+    fast_pair_kind(k1, t1, r0, i0, r1, i1);  // along b1
+    fast_pair_kind(k1, t1, r2, i2, r3, i3);
+    fast_pair_kind(k2, t2, r0, i0, r2, i2);  // along b2
+    fast_pair_kind(k2, t2, r1, i1, r3, i3);
+    sre[e0] = r0; sim[e0] = i0;
+    sre[e1] = r1; sim[e1] = i1;
+    sre[e2] = r2; sim[e2] = i2;
+    sre[e3] = r3; sim[e3] = i3;
+  }
+}
+
+__device__ __forceinline__ void tile_lazy2_pm(const TileGate& g, const double2* tab, uint64_t base, double* sre,
+                                              double* sim, uint32_t nblocks) {
+  switch (g.pm) {
+    case 2: tile_lazy2<2>(g, tab, base, sre, sim, nblocks); break;
+    case 3: tile_lazy2<3>(g, tab, base, sre, sim, nblocks); break;
+    case 4: tile_lazy2<4>(g, tab, base, sre, sim, nblocks); break;
+    case 5: tile_lazy2<5>(g, tab, base, sre, sim, nblocks); break;
+    case 6: tile_lazy2<6>(g, tab, base, sre, sim, nblocks); break;
+    default: tile_lazy2<kPhaseMaxTerms>(g, tab, base, sre, sim, nblocks); break;
   }
 }
 
@@ -444,6 +519,9 @@ __device__ __forceinline__ void tile_pass_gates(const PassArgs& A, uint64_t base
       case TM_PHASE:
         if (g.npos) tile_phase_pm<1>(g, A.tables + g.ptab, base, sre, sim, nw);
         else tile_phase_pm<0>(g, A.tables + g.ptab, base, sre, sim, nw);
+        break;
+      case TM_LAZY2:
+        tile_lazy2_pm(g, A.tables + g.ptab, base, sre, sim, nw);
         break;
       case TM_DIAG_LOCAL:
       case TM_DIAG_GLOBAL: {
@@ -908,6 +986,87 @@ size_t mark_shuffle_runs(TileGate* g, size_t count, int k) {
   return in_runs;
 }
 
+// Fast mode: fuse consecutive lazy rotations on two distinct tile qubits,
+// both carrying a phase entry, into one TM_LAZY2 op, when the second op's
+// phase masks do not contain the first op's qubit (its phase then commutes
+// with the first rotation) and the two tables have at most kPhaseMaxTerms
+// masks between them.  pg[i] is the descriptor of gates[i]; the joint tables
+// are appended to `flat` (re, im pairs).  Returns the FP64 instructions
+// saved: 4 per block of four amplitudes, 2^n per fused pair.  SPZ_FAST_PAIRS=0
+// in the environment turns the fusion off (for A/B measurements).
+bool fast_pairs_enabled() {
+  static const bool on = [] {
+    const char* v = std::getenv("SPZ_FAST_PAIRS");
+    return !(v && v[0] == '0');
+  }();
+  return on;
+}
+
+bool lazy_with_table(const GateApp& g) {
+  return g.kind >= FK_LAZY_H && g.kind <= FK_LAZY_RY_B && g.table >= 0 && g.cond < 0 && g.ones == 0 &&
+         g.zeros == 0;
+}
+
+uint64_t fuse_lazy_pairs(std::vector<TileGate>& pg, const std::vector<GateApp>& gates,
+                         const std::vector<PhaseTable>& tables, std::vector<double>* flat, uint32_t n) {
+  if (!fast_pairs_enabled()) return 0;
+  std::vector<TileGate> out;
+  uint64_t saved = 0;
+  size_t i = 0;
+  while (i < pg.size()) {
+    if (i + 1 < pg.size() && lazy_with_table(gates[i]) && lazy_with_table(gates[i + 1]) &&
+        gates[i].target != gates[i + 1].target && pg[i].mode == TM_PAIR && pg[i + 1].mode == TM_PAIR) {
+      const PhaseTable& T1 = tables[gates[i].table];
+      const PhaseTable& T2 = tables[gates[i + 1].table];
+      const uint64_t q1b = 1ull << gates[i].target, q2b = 1ull << gates[i + 1].target;
+      bool ok = T1.m + T2.m <= kPhaseMaxTerms;
+      for (int j = 0; ok && j < T2.m; ++j) ok = (T2.mask[j] & q1b) == 0;
+      if (ok) {
+        TileGate t = pg[i];
+        const TileGate& u = pg[i + 1];
+        t.mode = TM_LAZY2;
+        t.kind2 = u.kind;
+        t.tbit2 = u.tbit;
+        t.c.sn = u.c.cs;
+        const int p1 = __builtin_ctz(t.tbit), p2 = __builtin_ctz(u.tbit);
+        t.npos = 2;
+        t.pos[0] = (uint8_t)std::min(p1, p2);
+        t.pos[1] = (uint8_t)std::max(p1, p2);
+        t.l_ones = 0;
+        t.e_mask = t.tbit | u.tbit;
+        t.pm1 = T1.m;
+        t.pm = T1.m + T2.m;
+        for (int j = 0; j < T2.m; ++j) {
+          t.pmask[T1.m + j] = u.pmask[j];
+          t.pemask[T1.m + j] = u.pemask[j];
+        }
+        uint32_t flip = 0;
+        for (int j = 0; j < T1.m; ++j)
+          if (T1.mask[j] & q2b) flip |= 1u << j;
+        t.ptab = (uint32_t)(flat->size() / 2);
+        const uint32_t E = 1u << t.pm;
+        for (uint32_t idx = 0; idx < E; ++idx) {
+          const uint32_t i1 = idx & ((1u << T1.m) - 1), i2 = idx >> T1.m;
+          const std::complex<double> w1(T1.re[i1], T1.im[i1]), w2(T2.re[i2], T2.im[i2]);
+          const std::complex<double> w3 = std::complex<double>(T1.re[i1 ^ flip], T1.im[i1 ^ flip]) * w2;
+          for (const std::complex<double>& w : {w1, w2, w3}) {
+            flat->push_back(w.real());
+            flat->push_back(w.imag());
+          }
+        }
+        out.push_back(t);
+        saved += 1ull << n;
+        i += 2;
+        continue;
+      }
+    }
+    out.push_back(pg[i]);
+    ++i;
+  }
+  pg.swap(out);
+  return saved;
+}
+
 }  // namespace
 
 namespace {
@@ -1241,16 +1400,23 @@ int run_gates_io(spz_state_t h, const std::vector<GateApp>& gates_in, uint32_t f
     return P.gates.size() > 1 || P.gates[0].kind >= FK_LAZY_H || P.gates[0].cond >= 0;
   };
   std::vector<TileGate> all;
-  std::vector<size_t> offs;
+  std::vector<size_t> offs, counts;
   for (const PlannedPass& P : passes) {
     offs.push_back(all.size());
+    std::vector<TileGate> pg;
     if (tiled(P)) {
-      for (const GateApp& g : P.gates) all.push_back(tile_gate(g, P.local, &tables, &table_offsets));
+      for (const GateApp& g : P.gates) pg.push_back(tile_gate(g, P.local, &tables, &table_offsets));
+      if (fast) {
+        const uint64_t saved = fuse_lazy_pairs(pg, P.gates, tables, &flat, n);
+        if (st) st->fp64_ops -= saved;
+      }
       if (flags & SPZ_EXEC_SHUFFLE) {
-        const size_t r = mark_shuffle_runs(all.data() + offs.back(), P.gates.size(), (int)P.local.size());
+        const size_t r = mark_shuffle_runs(pg.data(), pg.size(), (int)P.local.size());
         if (st) st->shuffle_gates += r;
       }
+      all.insert(all.end(), pg.begin(), pg.end());
     }
+    counts.push_back(pg.size());
   }
   TileGate* dgates = nullptr;
   const double2* dtables = nullptr;
@@ -1308,7 +1474,7 @@ int run_gates_io(spz_state_t h, const std::vector<GateApp>& gates_in, uint32_t f
     A.gates = dgates + offs[p];
     A.tables = dtables;
     A.outcomes = h->meas ? reinterpret_cast<const int32_t*>(h->meas + kMeasOutcomeOffset) : nullptr;
-    A.ngates = (int)P.gates.size();
+    A.ngates = (int)counts[p];
     const uint32_t T = 1u << A.k;
     const size_t smem = 2 * T * sizeof(double) + (size_t)(1u << A.nhigh) * sizeof(uint64_t);
     const int threads = h->tile_threads ? h->tile_threads
@@ -1635,11 +1801,15 @@ int plan_stats(uint32_t n, const spz_op* ops, size_t nops, uint32_t flags, spz_e
       const std::vector<uint32_t> no_offsets(tables.size(), 0);
       std::vector<PlannedPass> planned = plan(run, n, k, c, !fast);
       pad_tile_passes(planned, n, k);
+      std::vector<double> no_flat;
       for (const PlannedPass& P : planned) {
-        if ((flags & SPZ_EXEC_SHUFFLE) && (P.gates.size() > 1 || P.gates[0].kind >= FK_LAZY_H || P.gates[0].cond >= 0)) {
+        if ((fast || (flags & SPZ_EXEC_SHUFFLE)) &&
+            (P.gates.size() > 1 || P.gates[0].kind >= FK_LAZY_H || P.gates[0].cond >= 0)) {
           std::vector<TileGate> tg;
           for (const GateApp& g : P.gates) tg.push_back(tile_gate(g, P.local, &tables, &no_offsets));
-          st->shuffle_gates += mark_shuffle_runs(tg.data(), tg.size(), (int)P.local.size());
+          if (fast) st->fp64_ops -= fuse_lazy_pairs(tg, P.gates, tables, &no_flat, n);
+          if (flags & SPZ_EXEC_SHUFFLE) st->shuffle_gates += mark_shuffle_runs(tg.data(), tg.size(), (int)P.local.size());
+          no_flat.clear();
         }
         if (order && !fast)
           for (const GateApp& g : P.gates) {
@@ -1780,15 +1950,19 @@ int build_program(spz_program_t p, const spz_op* ops, size_t nops, uint32_t flag
     }
   }
   std::vector<TileGate> all;
-  std::vector<size_t> offs;
+  std::vector<size_t> offs, counts;
   for (const PlannedPass& P : planned) {
     offs.push_back(all.size());
     const bool tiled = P.gates.size() > 1 || P.gates[0].kind >= FK_LAZY_H || P.gates[0].cond >= 0;
+    std::vector<TileGate> pg;
     if (tiled) {
-      for (const GateApp& g : P.gates) all.push_back(tile_gate(g, P.local, &tables, &table_offsets));
+      for (const GateApp& g : P.gates) pg.push_back(tile_gate(g, P.local, &tables, &table_offsets));
+      if (fast) p->stats.fp64_ops -= fuse_lazy_pairs(pg, P.gates, tables, &flat, n);
       if (flags & SPZ_EXEC_SHUFFLE)
-        p->stats.shuffle_gates += mark_shuffle_runs(all.data() + offs.back(), P.gates.size(), (int)P.local.size());
+        p->stats.shuffle_gates += mark_shuffle_runs(pg.data(), pg.size(), (int)P.local.size());
+      all.insert(all.end(), pg.begin(), pg.end());
     }
+    counts.push_back(pg.size());
   }
   const size_t gbytes = (all.size() * sizeof(TileGate) + 255) / 256 * 256;
   const size_t tbytes = flat.size() * sizeof(double);
@@ -1818,7 +1992,7 @@ int build_program(spz_program_t p, const spz_op* ops, size_t nops, uint32_t flag
     A.ntiles = 1ull << (n - A.k);
     A.gates = (const TileGate*)p->dbuf + offs[q];
     A.tables = (const double2*)((char*)p->dbuf + gbytes);
-    A.ngates = (int)P.gates.size();
+    A.ngates = (int)counts[q];
     const uint32_t T = 1u << A.k;
     pp.smem = 2 * T * sizeof(double) + (size_t)(1u << A.nhigh) * sizeof(uint64_t);
     pp.threads = (int)std::min<uint32_t>(kTileThreads, std::max<uint32_t>(32, T / 2));

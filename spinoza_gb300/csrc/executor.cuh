@@ -26,7 +26,7 @@ constexpr int kTileLowBits = 3;   // qubits 0..2 always local: 64-byte contiguou
 #endif
 constexpr int kTileThreads = SPZ_TILE_THREADS;
 
-enum TileMode { TM_PAIR = 0, TM_DIAG_LOCAL = 1, TM_DIAG_GLOBAL = 2, TM_SWAP = 3, TM_PHASE = 4 };
+enum TileMode { TM_PAIR = 0, TM_DIAG_LOCAL = 1, TM_DIAG_GLOBAL = 2, TM_SWAP = 3, TM_PHASE = 4, TM_LAZY2 = 5 };
 
 struct TileGate {
   int32_t kind;
@@ -49,6 +49,14 @@ struct TileGate {
   uint32_t ptab;
   int32_t cond;  // >= 0: applies only if that qubit's device-side measurement read 1
   uint32_t e_mask;  // pos[0 .. npos - 1] as a bit mask of the tile offset
+  // TM_LAZY2 (fast mode): two lazy rotations with phase entries, `kind` on
+  // tbit (coefficient c.cs) then `kind2` on tbit2 (c.sn), fused over blocks
+  // of four amplitudes.  pmask / pemask [0 .. pm1) are the first op's phase
+  // masks, [pm1 .. pm) the second's; the table holds three entries per index
+  // (w1, w2, w1' w2), w1' being the first op's entry with its masks' tbit2
+  // parities flipped.
+  int32_t kind2;
+  int32_t pm1;
   // SPZ_EXEC_SHUFFLE: > this gate's index, the end of a run of gates that the
   // block applies with warp shuffles (circuit.cu, tile_run_shfl); 0 otherwise.
   int32_t run_end;

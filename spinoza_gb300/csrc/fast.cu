@@ -24,7 +24,9 @@
 //     remaining terms and G are applied in one table multiply.
 //
 // A brickwork layer of U gates then costs ~8 FP64 instructions per pair and
-// gate instead of 14.  Controlled gates other than CX stay exact.
+// gate instead of 14 (7 where the executor fuses two lazy ops over blocks of
+// four amplitudes, circuit.cu fuse_lazy_pairs).  Controlled gates other than
+// CX stay exact.
 #include <cmath>
 #include <complex>
 #include <vector>

@@ -66,8 +66,7 @@ __device__ __forceinline__ void gate_pair(const Coef& g, double& a, double& b, d
 // Fast-mode lazy ops (the gate divided by a scalar carried elsewhere): four
 // FP64 instructions per pair.  Coefficient in g.cs (t or u).
 template <int FK>
-__device__ __forceinline__ void fast_pair(const Coef& g, double& a, double& b, double& c, double& d) {
-  const double t = g.cs;
+__device__ __forceinline__ void fast_pair_t(const double t, double& a, double& b, double& c, double& d) {
   double na, nb, nc, nd;
   if constexpr (FK == FK_LAZY_H) {
     na = dadd(a, c); nb = dadd(b, d); nc = dsub(a, c); nd = dsub(b, d);
@@ -81,6 +80,22 @@ __device__ __forceinline__ void fast_pair(const Coef& g, double& a, double& b, d
     na = dfma(t, a, dneg(c)); nb = dfma(t, b, dneg(d)); nc = dfma(t, c, a); nd = dfma(t, d, b);
   }
   a = na; b = nb; c = nc; d = nd;
+}
+
+template <int FK>
+__device__ __forceinline__ void fast_pair(const Coef& g, double& a, double& b, double& c, double& d) {
+  fast_pair_t<FK>(g.cs, a, b, c, d);
+}
+
+// A lazy op whose kind is known only at run time (uniform over the block).
+__device__ __forceinline__ void fast_pair_kind(int kind, double t, double& a, double& b, double& c, double& d) {
+  switch (kind) {
+    case FK_LAZY_H: fast_pair_t<FK_LAZY_H>(t, a, b, c, d); break;
+    case FK_LAZY_RX_A: fast_pair_t<FK_LAZY_RX_A>(t, a, b, c, d); break;
+    case FK_LAZY_RX_B: fast_pair_t<FK_LAZY_RX_B>(t, a, b, c, d); break;
+    case FK_LAZY_RY_A: fast_pair_t<FK_LAZY_RY_A>(t, a, b, c, d); break;
+    default: fast_pair_t<FK_LAZY_RY_B>(t, a, b, c, d); break;
+  }
 }
 
 // Diagonal gates on one amplitude; `one` is the amplitude's target bit.
