@@ -518,6 +518,10 @@ def gpu_arm(args) -> None:
         sweep = sweep_single_qubit(state, n, peaks["hbm_gbs"], fma_rate)
     adj = None if args.no_adjoint or rank != 0 else adjoint_bench()
     bat = None if args.no_batch or rank != 0 else batch_bench(args)
+    qft = mea = None
+    if rank == 0 and not args.no_configs:
+        qft = qft20_bench(args)
+        mea = measure28_bench(args)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         torch.cuda.synchronize()
@@ -578,6 +582,8 @@ def gpu_arm(args) -> None:
             "clocks": clk.summary(),
             "adjoint": adj,
             "batch": bat,
+            "qft20": qft,
+            "measure28": mea,
         }
         print(json.dumps(line), flush=True)
     if dist:
@@ -662,8 +668,10 @@ def workload_narrow(args) -> None:
           staging=args.staging, modes=out, dfma_rate=rate, higher_is_better=True)
 
 
-def workload_qft20(args) -> None:
-    """QFT with swaps on a seeded N(0,1) normalised 20-qubit state."""
+def qft20_bench(args) -> dict:
+    """QFT with swaps on a seeded N(0,1) normalised 20-qubit state: the fused
+    executor, the unfused per-gate path and compiled programs (graph replay),
+    exact and fast, against the oracle."""
     import oracle
     from spinoza_gb300 import _native as nat
     from spinoza_gb300 import circuit, rng
@@ -714,20 +722,26 @@ def workload_qft20(args) -> None:
     d_fast = float(max(np.max(np.abs(gre - re)), np.max(np.abs(gim - im))))
     d = float(max(np.max(np.abs(pre - re)), np.max(np.abs(pim - im))))
     abytes = algorithmic_bytes(ops, n)
-    _line("QFT-20 circuit time", out["program_fast"] * 1e3, "ms", args, higher_is_better=False,
-          config={"workload": "QFT with swaps, 20 qubits, N(0,1) normalised state seed 1", "gates": len(ops)},
-          execute_ms=out["fused"] * 1e3, unfused_ms=out["unfused"] * 1e3,
-          effective_gbs=abytes / out["program_fast"] / 1e9,
-          passes=circuit.plan_stats(n, ops)["passes"], cpu_baseline_ms=t_cpu * 1e3, cpu_threads=oracle.num_threads(),
-          program_ms=out["program"] * 1e3, program_fast_ms=out["program_fast"] * 1e3,
-          max_abs_diff_vs_oracle=d, bit_identical=bool(d == 0.0), max_abs_diff_fast_vs_oracle=d_fast,
-          note="value: the fast-mode program (planned once, replayed as a CUDA graph); execute_ms: the bit-exact "
-               "spz_circuit_execute (plans each run); program_ms: the bit-exact program; every run includes a "
-               "device copy of the input state")
+    return {"workload": "QFT with swaps, 20 qubits, N(0,1) normalised state seed 1", "gates": len(ops),
+            "program_fast_ms": out["program_fast"] * 1e3, "program_ms": out["program"] * 1e3,
+            "execute_ms": out["fused"] * 1e3, "unfused_ms": out["unfused"] * 1e3,
+            "effective_gbs": abytes / out["program_fast"] / 1e9, "passes": circuit.plan_stats(n, ops)["passes"],
+            "cpu_baseline_ms": t_cpu * 1e3, "cpu_threads": oracle.num_threads(),
+            "max_abs_diff_vs_oracle": d, "bit_identical": bool(d == 0.0), "max_abs_diff_fast_vs_oracle": d_fast,
+            "note": "program_fast: the fast-mode program (planned once, replayed as a CUDA graph); execute: the "
+                    "bit-exact spz_circuit_execute (plans each run); program: the bit-exact program; every run "
+                    "includes a device copy of the input state; cpu_baseline: the oracle, one run"}
 
 
-def workload_measure28(args) -> None:
-    """28 qubits: 1e6 seeded shots (bit-exact rule) and <H> = sum a ZZ + b X."""
+def workload_qft20(args) -> None:
+    r = qft20_bench(args)
+    _line("QFT-20 circuit time", r["program_fast_ms"], "ms", args, higher_is_better=False,
+          config={"workload": r.pop("workload"), "gates": r.pop("gates")}, **r)
+
+
+def measure28_bench(args, oracle_check: bool = True) -> dict:
+    """28 qubits: 1e6 seeded shots (bit-exact rule) and <H> = sum a ZZ + b X,
+    with the oracle's shots and <H> on the same downloaded state."""
     from spinoza_gb300 import core, rng
     from spinoza_gb300.core import State
 
@@ -742,11 +756,31 @@ def workload_measure28(args) -> None:
     H = core.ising_hamiltonian(a, b)
     t_h = _event_time(lambda: core.pauli_expectation(s, H), args.steps, 1)
     N = 1 << n
-    _line("shots/s at 28 qubits", 1e6 / t_shots, "shots/s", args, higher_is_better=True,
-          config={"workload": "28-qubit N(0,1) normalised state, 1e6 shots (uniform seed 4), <H> with "
-                              "a_i, b_i ~ N(0,1) (seed 5)", "terms": int(len(H))},
-          sample_ms=t_shots * 1e3, sample_gbs=(24 * N) / t_shots / 1e9, expectation_ms=t_h * 1e3,
-          expectation_gbs=(16 * N) / t_h / 1e9, energy=core.pauli_expectation(s, H))
+    energy = core.pauli_expectation(s, H)
+    out = {"workload": "28-qubit N(0,1) normalised state, 1e6 shots (uniform seed 4), <H> with a_i, b_i ~ N(0,1) "
+                       "(seed 5)", "terms": int(len(H)), "shots_per_s": 1e6 / t_shots, "sample_ms": t_shots * 1e3,
+           "sample_gbs": (24 * N) / t_shots / 1e9, "expectation_ms": t_h * 1e3,
+           "expectation_gbs": (16 * N) / t_h / 1e9, "energy": energy}
+    if oracle_check:
+        import oracle
+
+        shots = core.sample(s, u)
+        re, im = s.to_numpy()
+        del s
+        t0 = time.perf_counter()
+        want = oracle.sample(re, im, u)
+        t_cpu = time.perf_counter() - t0
+        e_orc = oracle.pauli_expectation(re, im, H)
+        out.update({"shots_bit_identical_vs_oracle": bool(np.array_equal(shots, want)),
+                    "energy_abs_diff_vs_oracle": abs(energy - e_orc), "cpu_sample_ms": t_cpu * 1e3,
+                    "cpu_threads": oracle.num_threads()})
+    return out
+
+
+def workload_measure28(args) -> None:
+    r = measure28_bench(args, oracle_check=False)
+    _line("shots/s at 28 qubits", r["shots_per_s"], "shots/s", args, higher_is_better=True,
+          config={"workload": r.pop("workload"), "terms": r.pop("terms")}, **r)
 
 
 def batch_bench(args) -> dict:
@@ -919,6 +953,8 @@ def main() -> None:
     ap.add_argument("--no-autotune", action="store_true",
                     help="batch: the library's default launch shape instead of the cached autotuner's choice")
     ap.add_argument("--no-batch", action="store_true", help="headline line without the 4096-instance batch object")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="headline line without the QFT-20 and 28-qubit measurement objects")
     ap.add_argument("--batch-steps", type=int, default=1, help="timed runs of the 4096-instance batch")
     ap.add_argument("--batch-tpi", type=int, default=0, help="batch workload: tiles per work item of a wide instance")
     ap.add_argument("--batch-apart", action="store_true", help="batch workload: wide instances one at a time")
