@@ -545,13 +545,16 @@ __device__ __forceinline__ void tile_pass_gates(const PassArgs& A, uint64_t base
 }
 
 template <bool SHFL>
-__global__ void __launch_bounds__(kTileThreads, SPZ_TILE_MIN_BLOCKS) tile_kernel(PassArgs A) {
+__global__ void __launch_bounds__(kTileThreads, SHFL ? 12 : SPZ_TILE_MIN_BLOCKS) tile_kernel(PassArgs A) {
   extern __shared__ double smem[];
   const int K = A.k;
   const uint32_t T = 1u << K;
   double* sre = smem;
   double* sim = smem + T;
-  uint64_t* rowoff = reinterpret_cast<uint64_t*>(smem + 2 * T);
+  // Row offsets >> c (their bits are local qubits >= c, so 32 bits hold them
+  // for up to 34 qubits): half the shared memory of 64-bit entries, which
+  // lets a 13th block of 2^10-amplitude tiles onto an SM.
+  uint32_t* rowoff = reinterpret_cast<uint32_t*>(smem + 2 * T);
   const uint32_t nrows = 1u << A.nhigh;
   const uint32_t cmask = (1u << A.c) - 1;
   // Row offsets: scatter of the high local bits, the same for every tile.
@@ -564,7 +567,7 @@ __global__ void __launch_bounds__(kTileThreads, SPZ_TILE_MIN_BLOCKS) tile_kernel
     uint64_t off = 0;
     for (int j = 0; j < A.nhigh; ++j)
       if ((r >> j) & 1) off |= 1ull << A.lpos[A.c + j];
-    rowoff[r] = off;
+    rowoff[r] = (uint32_t)(off >> A.c);
   }
   __syncthreads();
   for (uint64_t tile = A.tile_begin + blockIdx.x; tile < A.ntiles; tile += gridDim.x) {
@@ -572,7 +575,7 @@ __global__ void __launch_bounds__(kTileThreads, SPZ_TILE_MIN_BLOCKS) tile_kernel
     // load (pairs of consecutive amplitudes: c >= 1)
     for (uint32_t e2 = threadIdx.x; e2 < T / 2; e2 += blockDim.x) {
       const uint32_t e = 2 * e2;
-      const uint64_t gi = base | rowoff[e >> A.c] | (e & cmask);
+      const uint64_t gi = base | ((uint64_t)rowoff[e >> A.c] << A.c) | (e & cmask);
       double2 r = *reinterpret_cast<const double2*>(A.re + gi);
       double2 m = *reinterpret_cast<const double2*>(A.im + gi);
       // e even: e and e + 1 share a 16-byte slot, in reverse order when the
@@ -590,7 +593,7 @@ __global__ void __launch_bounds__(kTileThreads, SPZ_TILE_MIN_BLOCKS) tile_kernel
     // store
     for (uint32_t e2 = threadIdx.x; e2 < T / 2; e2 += blockDim.x) {
       const uint32_t e = 2 * e2;
-      const uint64_t gi = base | rowoff[e >> A.c] | (e & cmask);
+      const uint64_t gi = base | ((uint64_t)rowoff[e >> A.c] << A.c) | (e & cmask);
       const uint32_t p = TileSwizzle::at(e) & ~1u;
       double2 r = *reinterpret_cast<const double2*>(sre + p);
       double2 m = *reinterpret_cast<const double2*>(sim + p);
@@ -1476,7 +1479,7 @@ int run_gates_io(spz_state_t h, const std::vector<GateApp>& gates_in, uint32_t f
     A.outcomes = h->meas ? reinterpret_cast<const int32_t*>(h->meas + kMeasOutcomeOffset) : nullptr;
     A.ngates = (int)counts[p];
     const uint32_t T = 1u << A.k;
-    const size_t smem = 2 * T * sizeof(double) + (size_t)(1u << A.nhigh) * sizeof(uint64_t);
+    const size_t smem = 2 * T * sizeof(double) + (size_t)(1u << A.nhigh) * sizeof(uint32_t);
     const int threads = h->tile_threads ? h->tile_threads
                                         : (int)std::min<uint32_t>(kTileThreads, std::max<uint32_t>(32, T / 2));
     int resident = 0, sms = 0;
@@ -1994,7 +1997,7 @@ int build_program(spz_program_t p, const spz_op* ops, size_t nops, uint32_t flag
     A.tables = (const double2*)((char*)p->dbuf + gbytes);
     A.ngates = (int)counts[q];
     const uint32_t T = 1u << A.k;
-    pp.smem = 2 * T * sizeof(double) + (size_t)(1u << A.nhigh) * sizeof(uint64_t);
+    pp.smem = 2 * T * sizeof(double) + (size_t)(1u << A.nhigh) * sizeof(uint32_t);
     pp.threads = (int)std::min<uint32_t>(kTileThreads, std::max<uint32_t>(32, T / 2));
     pp.shfl = (flags & SPZ_EXEC_SHUFFLE) != 0;
     int resident = 0, sms = 0;

@@ -17,12 +17,15 @@ constexpr int kTileLowBits = 3;   // qubits 0..2 always local: 64-byte contiguou
 // the FP64 pipe stays busier with many independent small blocks per SM than
 // with a few large ones.  Measured on the 30-qubit brickwork, fast mode, share
 // of the DFMA issue rate: 2^12 tiles x 256 threads x 3 blocks 0.81; 2^11 x 128
-// x 6 0.84; 2^10 x 64 x 12 0.86 (exact mode 0.86-0.87 for all three).
+// x 6 0.84; 2^10 x 64 x 12 0.86 (exact mode 0.86-0.87 for all three).  With
+// 32-bit row offsets a block needs 16.5 KiB (+1 KiB the runtime reserves), so
+// 13 fit an SM's 228 KiB; 13 against 12 measured the same on the 30-qubit
+// brickwork (fast 4,472 / 4,476 ms, exact 8,360 / 8,355 ms per step).
 #ifndef SPZ_TILE_THREADS
 #define SPZ_TILE_THREADS 64
 #endif
 #ifndef SPZ_TILE_MIN_BLOCKS
-#define SPZ_TILE_MIN_BLOCKS 12  // 12 x (16 KiB tile + 1 KiB row table) fit one SM's shared memory
+#define SPZ_TILE_MIN_BLOCKS 13  // 13 x (16 KiB tile + 0.5 KiB row table + 1 KiB reserved) <= 228 KiB
 #endif
 constexpr int kTileThreads = SPZ_TILE_THREADS;
 
