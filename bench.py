@@ -551,6 +551,10 @@ def gpu_arm(args) -> None:
         if parity is None:
             parity = {}
         parity["vs_oracle"] = out
+    sw33 = None
+    if rank == 0 and not args.no_sweep33:
+        torch.cuda.empty_cache()
+        sw33 = sweep33_bench(33, steps=2, warmup=1)
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -584,6 +588,7 @@ def gpu_arm(args) -> None:
             "batch": bat,
             "qft20": qft,
             "measure28": mea,
+            "sweep33": sw33,
         }
         print(json.dumps(line), flush=True)
     if dist:
@@ -897,15 +902,15 @@ def workload_gate(args) -> None:
           ms=dt * 1e3, hbm_frac=gbs / peaks["hbm_gbs"], peak_gbs=peaks["hbm_gbs"])
 
 
-def workload_sweep33(args) -> None:
-    """Per-gate sweep: H, RZ, CX and 3-control X on every target at 33 qubits (128 GiB)."""
+def sweep33_bench(n: int = 33, steps: int = 3, warmup: int = 3) -> dict:
+    """Per-gate sweep: H, RZ, CX and 3-control X on every target at n qubits
+    (33: 128 GiB), the reference's arithmetic through the per-gate entry points."""
     import torch
 
     from spinoza_gb300 import gates as G
     from spinoza_gb300.core import State
     from spinoza_gb300.gates import Gate
 
-    n = args.qubits if args.qubits != 30 else 33
     N = 1 << n
     re = torch.empty(N, dtype=torch.float64, device="cuda")
     im = torch.empty(N, dtype=torch.float64, device="cuda")
@@ -919,9 +924,10 @@ def workload_sweep33(args) -> None:
              ("MCX3", lambda t: G.mc_apply(Gate.X, s, [(t + 1) % n, (t + 2) % n, (t + 3) % n], None, t), 4)]
     for name, fn, bpn in kinds:
         for t in range(n):
-            dt = _event_time(lambda: fn(t), args.steps, args.warmup)
+            dt = _event_time(lambda: fn(t), steps, warmup)
             gbs = bpn * N / dt / 1e9
             rows.append({"gate": name, "target": t, "ms": dt * 1e3, "gbs": gbs, "frac": gbs / peaks["hbm_gbs"]})
+    del s, re, im
     summary = {}
     for name, _, _ in kinds:
         r = [x for x in rows if x["gate"] == name]
@@ -929,10 +935,17 @@ def workload_sweep33(args) -> None:
                          "gbs_median": statistics.median(x["gbs"] for x in r),
                          "frac_median": statistics.median(x["frac"] for x in r),
                          "frac_min": min(x["frac"] for x in r)}
-    _line(f"per-gate sweep at {n} qubits", summary["H"]["gbs_median"], "GB/s", args, higher_is_better=True,
-          config={"workload": f"H, RZ(0.7), CX(control (t+1) mod n), X with 3 controls (t+1..t+3 mod n), "
-                              f"targets 0..{n - 1}, {n} qubits ({16 * N >> 30} GiB)"},
-          summary=summary, rows=rows, peak_gbs=peaks["hbm_gbs"])
+    return {"workload": f"H, RZ(0.7), CX(control (t+1) mod n), X with 3 controls (t+1..t+3 mod n), targets "
+                        f"0..{n - 1}, {n} qubits ({16 * N >> 30} GiB)", "qubits": n, "steps": steps, "warmup": warmup,
+            "summary": summary, "rows": rows, "peak_gbs": peaks["hbm_gbs"],
+            "note": "GB/s = algorithmic bytes (32 N for H and RZ, 16 N for CX, 4 N for 3-control X) / CUDA-event "
+                    "time per application; the reference's arithmetic (exact kernels)"}
+
+
+def workload_sweep33(args) -> None:
+    r = sweep33_bench(args.qubits if args.qubits != 30 else 33, args.steps, args.warmup)
+    _line(f"per-gate sweep at {r['qubits']} qubits", r["summary"]["H"]["gbs_median"], "GB/s", args,
+          higher_is_better=True, config={"workload": r.pop("workload")}, **r)
 
 
 def main() -> None:
@@ -972,6 +985,7 @@ def main() -> None:
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-parity", action="store_true")
     ap.add_argument("--no-sweep", action="store_true", help="skip the per-gate sweep at the headline's qubit count")
+    ap.add_argument("--no-sweep33", action="store_true", help="skip the per-gate sweep at 33 qubits (128 GiB)")
     ap.add_argument("--exact", action="store_true", help="time the bit-exact executor mode instead of fast mode")
     ap.add_argument("--staging", default="threads", choices=["threads", "tma", "tma-prefetch", "shuffle"],
                     help="how fused passes stage their tiles: thread loads (default), TMA gathers, or "
