@@ -241,6 +241,8 @@ typedef struct spz_exec_stats {
   double tile_ms;          /* SPZ_EXEC_TIME_PASSES: device time of the tile passes  */
   double plain_ms;         /* SPZ_EXEC_TIME_PASSES: device time of plain gate passes */
   uint64_t shuffle_gates;  /* SPZ_EXEC_SHUFFLE: ops applied in warp-shuffle runs     */
+  uint64_t io_slab_passes; /* spz_circuit_execute_host: passes run slab by slab with
+                              the host copies overlapped                          */
 } spz_exec_stats;
 
 /* QuantumCircuit::execute (circuit.rs:552-600): apply `ops` in order.

@@ -75,7 +75,8 @@ class spz_tracker(ctypes.Structure):
 class spz_exec_stats(ctypes.Structure):
     _fields_ = [("gates", c_uint64), ("passes", c_uint64), ("tile_passes", c_uint64),
                 ("bytes_moved", c_uint64), ("algorithmic_bytes", c_uint64), ("fp64_ops", c_uint64),
-                ("tile_ms", c_double), ("plain_ms", c_double), ("shuffle_gates", c_uint64)]
+                ("tile_ms", c_double), ("plain_ms", c_double), ("shuffle_gates", c_uint64),
+                ("io_slab_passes", c_uint64)]
 
 
 class spz_pauli_term(ctypes.Structure):

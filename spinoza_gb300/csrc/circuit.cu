@@ -47,7 +47,20 @@ struct PassArgs {
   int c;            // low contiguous local qubits (0..c-1)
   int nhigh;        // k - c
   uint8_t lpos[kTileMaxK];  // sorted local qubits
+  // slab_on != 0: the launch covers only the tiles whose three tile-index bits
+  // at slab_pos (the non-local qubits of one host-copy slab) read `slab`; the
+  // loop index t then runs over the other tile-index bits.
+  uint32_t slab_on;
+  uint32_t slab_pos;
+  uint32_t slab;
 };
+
+// The tile index of loop index t (see PassArgs::slab_on).
+__device__ __forceinline__ uint64_t slab_tile(const PassArgs& A, uint64_t t) {
+  if (!A.slab_on) return t;
+  const uint32_t sp = A.slab_pos;
+  return ((t >> sp) << (sp + 3)) | ((uint64_t)A.slab << sp) | (t & ((1ull << sp) - 1));
+}
 
 // ------------------------------------------------------------ device side
 // Nibble-swizzled tile layout: removes the 2-way bank conflicts of pair ops on
@@ -570,8 +583,8 @@ __global__ void __launch_bounds__(kTileThreads, SHFL ? 12 : SPZ_TILE_MIN_BLOCKS)
     rowoff[r] = (uint32_t)(off >> A.c);
   }
   __syncthreads();
-  for (uint64_t tile = A.tile_begin + blockIdx.x; tile < A.ntiles; tile += gridDim.x) {
-    const uint64_t base = deposit(tile, A.lpos, K);
+  for (uint64_t t = A.tile_begin + blockIdx.x; t < A.ntiles; t += gridDim.x) {
+    const uint64_t base = deposit(slab_tile(A, t), A.lpos, K);
     // load (pairs of consecutive amplitudes: c >= 1)
     for (uint32_t e2 = threadIdx.x; e2 < T / 2; e2 += blockDim.x) {
       const uint32_t e = 2 * e2;
@@ -1289,6 +1302,12 @@ int io_copy_slab(spz_state_t h, double* dre, double* dim, const double* sre, con
     return SPZ_OK;
   }
   const uint64_t runs = 1ull << (h->n - q - 3), len = 1ull << q;
+  if (runs > (uint64_t)kIoMaxRuns) {  // one strided copy per array: rows of 2^q amplitudes, pitch 2^(q+3)
+    const size_t width = len * sizeof(double), pitch = width << 3, off = (size_t)j << q;
+    SPZ_CUDA(cudaMemcpy2DAsync(dre + off, pitch, sre + off, pitch, width, runs, kind, h->copy_stream));
+    SPZ_CUDA(cudaMemcpy2DAsync(dim + off, pitch, sim + off, pitch, width, runs, kind, h->copy_stream));
+    return SPZ_OK;
+  }
   for (uint64_t r = 0; r < runs; ++r) {
     const uint64_t off = (r << (q + 3)) | ((uint64_t)j << q);
     SPZ_CUDA(cudaMemcpyAsync(dre + off, sre + off, len * sizeof(double), kind, h->copy_stream));
@@ -1461,7 +1480,9 @@ int run_gates_io(spz_state_t h, const std::vector<GateApp>& gates_in, uint32_t f
     if (rc) return rc;
   }
   // Tiles [part * ntiles / parts, (part + 1) * ntiles / parts) of tile pass p.
-  auto launch_tiles = [&](size_t p, int part, int parts) -> int {
+  // slab_q >= 0: slab `part` of kIoChunks whose slab qubits slab_q .. slab_q + 2
+  // are non-local in pass p (the tiles are selected by their index bits).
+  auto launch_tiles = [&](size_t p, int part, int parts, int slab_q = -1) -> int {
     const PlannedPass& P = passes[p];
     PassArgs A{};
     A.re = h->re;
@@ -1471,9 +1492,20 @@ int run_gates_io(spz_state_t h, const std::vector<GateApp>& gates_in, uint32_t f
     A.nhigh = A.k - c;
     for (int j = 0; j < A.k; ++j) A.lpos[j] = (uint8_t)P.local[j];
     const uint64_t ntiles = 1ull << (n - A.k);
-    const uint64_t per = ntiles / parts;
-    A.tile_begin = per * part;
-    A.ntiles = per * (part + 1);
+    uint64_t per = ntiles / parts;
+    if (slab_q >= 0) {
+      uint64_t L = 0;
+      for (int q : P.local) L |= 1ull << q;
+      A.slab_on = 1;
+      A.slab_pos = (uint32_t)(slab_q - __builtin_popcountll(L & ((1ull << slab_q) - 1)));
+      A.slab = (uint32_t)part;
+      per = ntiles / kIoChunks;
+      A.tile_begin = 0;
+      A.ntiles = per;
+    } else {
+      A.tile_begin = per * part;
+      A.ntiles = per * (part + 1);
+    }
     A.gates = dgates + offs[p];
     A.tables = dtables;
     A.outcomes = h->meas ? reinterpret_cast<const int32_t*>(h->meas + kMeasOutcomeOffset) : nullptr;
@@ -1485,7 +1517,7 @@ int run_gates_io(spz_state_t h, const std::vector<GateApp>& gates_in, uint32_t f
     int resident = 0, sms = 0;
     int rc = tile_launch_shape(h->device, threads, smem, &resident, &sms, shfl);
     if (rc) return rc;
-    if (use_tma && A.c == kTileLowBits && A.k >= kTileLowBits + 2) {
+    if (use_tma && !A.slab_on && A.c == kTileLowBits && A.k >= kTileLowBits + 2) {
       const bool pre = (flags & SPZ_EXEC_TMA_PREFETCH) != 0;
       const size_t tsmem = (pre ? 4 : 2) * T * sizeof(double) + (size_t)(1u << A.nhigh) * sizeof(uint64_t) + 128;
       int tres = 0;
@@ -1540,11 +1572,45 @@ int run_gates_io(spz_state_t h, const std::vector<GateApp>& gates_in, uint32_t f
         st->passes += m;
         st->tile_passes += m;
         st->bytes_moved += m * (32ull << n);
+        st->io_slab_passes += m;
       }
       first = m;
     }
   }
-  for (size_t p = first; p < passes.size(); ++p) {
+  // Slab-major suffix: the trailing tile passes that all keep three
+  // consecutive qubits q .. q + 2 non-local run slab by slab (passes s .. last
+  // on slab j, then slab j's download), so the download hides behind several
+  // passes instead of the last one.  q is the one that gives the longest
+  // suffix (the highest among equals); its slabs are copied as up to 64 runs
+  // (q >= n - 9) or as one strided copy of rows of 2^q amplitudes
+  // (15 <= q <= 24).  Rows of 2^11 amplitudes (16 KiB) measured about half
+  // the contiguous copy rate (2 GiB slabs in 20 ms against 10 ms); rows of at
+  // least 256 KiB keep the per-row cost negligible.
+  size_t suf = passes.size();
+  int suf_q = -1;
+  if (io && io->out_re && !use_tma && passes.size() > first) {
+    const size_t room = passes.size() - first - (io->in_re && !uploaded_wait ? 1 : 0);
+    size_t best = 1;
+    for (int q = (int)n - 3; q >= 3; --q) {
+      if ((int)n - q - 3 > 6 && (q < 15 || q > 24)) continue;
+      const uint64_t slab_bits = 7ull << q;
+      size_t m = 0;
+      while (m < room) {
+        const PlannedPass& P = passes[passes.size() - 1 - m];
+        if (!tiled(P)) break;
+        uint64_t L = 0;
+        for (int x : P.local) L |= 1ull << x;
+        if (L & slab_bits) break;
+        ++m;
+      }
+      if (m > best) {
+        best = m;
+        suf_q = q;
+      }
+    }
+    if (suf_q >= 0) suf = passes.size() - best;
+  }
+  for (size_t p = first; p < suf; ++p) {
     const PlannedPass& P = passes[p];
     const bool last = p + 1 == passes.size();
     if (!tiled(P)) {
@@ -1600,6 +1666,7 @@ int run_gates_io(spz_state_t h, const std::vector<GateApp>& gates_in, uint32_t f
       }
     }
     if (split_in) uploaded_wait = true;
+    if (st && launches > 1) st->io_slab_passes++;
     rc = timer.end(true);
     if (!rc && last && !split_out) rc = download_all();
     if (rc) {
@@ -1610,6 +1677,29 @@ int run_gates_io(spz_state_t h, const std::vector<GateApp>& gates_in, uint32_t f
       st->passes++;
       st->tile_passes++;
       st->bytes_moved += 32ull << n;
+    }
+  }
+  if (suf < passes.size()) {
+    const size_t m = passes.size() - suf;
+    int rc = wait_all_uploads();
+    if (!rc) rc = timer.begin();
+    for (int j = 0; j < kIoChunks && !rc; ++j) {
+      for (size_t p = suf; p < passes.size() && !rc; ++p) rc = launch_tiles(p, j, kIoChunks, suf_q);
+      if (!rc) {
+        cudaError_t re = cudaEventRecord(io->down[j], h->stream);
+        rc = re == cudaSuccess ? io_download(h, io, j, suf_q) : cuda_fail(re, "cudaEventRecord");
+      }
+    }
+    if (!rc) rc = timer.end(true);
+    if (rc) {
+      timer.collect(nullptr);
+      return rc;
+    }
+    if (st) {
+      st->passes += m;
+      st->tile_passes += m;
+      st->bytes_moved += m * (32ull << n);
+      st->io_slab_passes += m;
     }
   }
   int rc = timer.collect(st);

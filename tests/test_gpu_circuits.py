@@ -368,6 +368,49 @@ def test_execute_host_slab_major_passes(gpu, case, fast):
         assert st.gates == len(ops) and st.tile_passes >= 2
 
 
+def _gap_brickwork(n, layers, gap=(15, 16, 17)):
+    """Brickwork over every qubit but those in `gap`, which no gate touches:
+    the trailing passes keep the gap non-local while the top qubits are local,
+    so the download runs as a slab-major suffix in the gap's geometry (rows of
+    2^15 amplitudes: 2^(n-18) of them per slab, as separate copies up to 64 and
+    as one strided copy beyond)."""
+    qs = [q for q in range(n) if q not in gap]
+    qc = _builder()
+    ang = rng.uniforms(23, 3 * len(qs) * layers) * 2 * math.pi
+    k = 0
+    for _ in range(layers):
+        for q in qs:
+            qc.u(ang[k], ang[k + 1], ang[k + 2], q)
+            k += 3
+        for a, b in zip(qs[0::2], qs[1::2]):
+            qc.cx(a, b)
+        for a, b in zip(qs[1::2], qs[2::2]):
+            qc.cx(a, b)
+    return qc.ops()
+
+
+@pytest.mark.parametrize("fast", [False, True], ids=["exact", "fast"])
+@pytest.mark.parametrize("case", ["gap20", "gap25", "brickwork"])
+def test_execute_host_slab_major_suffix(gpu, case, fast):
+    """Trailing passes that keep three consecutive qubits non-local run slab by
+    slab with each slab's download right after its last pass: results equal
+    the device execute bit for bit, in place and into separate arrays."""
+    n = 25 if case == "gap25" else 20
+    ops = _gap_brickwork(n, 3) if case != "brickwork" else brickwork(n, 2)
+    init = rng.normal_state(n, 29)
+    s = State.from_arrays(*init)
+    QuantumCircuit.from_state(s, fast=fast).execute_ops(ops)
+    want = s.to_numpy()
+    for inplace in (True, False):
+        re, im = _host_pair(init, True)
+        out = None if inplace else _host_pair((np.zeros_like(init[0]), np.zeros_like(init[1])), True)
+        st = circuit.execute_host(ops, re, im, out, fast=fast)
+        got = (re, im) if inplace else out
+        assert np.array_equal(got[0], want[0]) and np.array_equal(got[1], want[1])
+        if case != "brickwork":
+            assert st.io_slab_passes >= 4, st.io_slab_passes
+
+
 @pytest.mark.parametrize("fast", [False, True], ids=["exact", "fast"])
 def test_execute_host_with_measurements(gpu, fast):
     """Measurements split the run into segments: the upload feeds the first,

@@ -41,7 +41,7 @@ def test_struct_layouts():
     assert ctypes.sizeof(nat.spz_gate) == 40
     assert ctypes.sizeof(nat.spz_op) == 64
     assert ctypes.sizeof(nat.spz_pauli_term) == 24
-    assert ctypes.sizeof(nat.spz_exec_stats) == 72
+    assert ctypes.sizeof(nat.spz_exec_stats) == 80
 
 
 def test_rng_stream_matches_oracle():
