@@ -260,9 +260,11 @@ int spz_circuit_execute(spz_state_t h, const spz_op* ops, size_t nops, spz_track
  * reference's in-place behaviour.  For page-locked arrays (cudaHostAlloc /
  * cudaHostRegister) the upload is cut into 8 slabs that the leading tile
  * passes consume as they arrive (every leading pass that keeps the slab
- * qubits non-local runs slab by slab) and the download follows the last pass
- * slab by slab, on a second stream; pageable arrays are copied whole before
- * and after.  Same flags, tracker and stats as spz_circuit_execute. */
+ * qubits non-local runs slab by slab) and the download follows the trailing
+ * passes slab by slab (every trailing pass that keeps three consecutive
+ * qubits non-local runs slab by slab), on a second stream; pageable arrays
+ * are copied whole before and after.  Same flags, tracker and stats as
+ * spz_circuit_execute (stats->io_slab_passes counts the slab-by-slab passes). */
 int spz_circuit_execute_host(spz_state_t h, const double* in_reals, const double* in_imags, double* out_reals,
                              double* out_imags, const spz_op* ops, size_t nops, spz_tracker* tracker,
                              uint32_t flags, spz_exec_stats* stats);
