@@ -485,8 +485,8 @@ def gpu_arm(args) -> None:
                "upload_alone_ms": 1e3 * (t2 - t1), "download_alone_ms": 1e3 * (t3 - t2),
                "h2d_gbs": 16 * N / (t2 - t1) / 1e9, "d2h_gbs": 16 * N / (t3 - t2) / 1e9,
                "h2d_gbs_torch_copy": 16 * N / min(tup) / 1e9, "host": numa,
-               "api": "spz_circuit_execute_host (pinned host arrays in and out; the copies overlap the first "
-                      "and last tile pass, slab by slab)"}
+               "api": "spz_circuit_execute_host (pinned host arrays in and out; the copies overlap the leading "
+                      "and trailing tile passes, slab by slab)"}
         del hin_re, hin_im, hout_re, hout_im
 
     # Parity at full size: the exact (reference-arithmetic, bit-identical to the
