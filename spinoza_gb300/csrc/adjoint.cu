@@ -719,6 +719,7 @@ using namespace spz;
 extern "C" int spz_adjoint_gradient(spz_state_t h, const spz_op* ops, size_t nops, const uint32_t* param_index,
                                     size_t nparams, const spz_pauli_term* terms, size_t nterms, uint32_t flags,
                                     double* energy, double* grad) {
+  NvtxRange range("spz_adjoint_gradient");
   if (!h) return fail(SPZ_ERR_NULL, "handle is NULL");
   if (int rc = settle(h)) return rc;
   return adjoint_gradient(h, ops, nops, param_index, nparams, terms, nterms, flags, energy, grad, nullptr, nullptr);

@@ -1283,6 +1283,7 @@ int spz_batch_create(const spz_batch_instance* instances, size_t ninstances, con
 }
 
 int spz_batch_run(spz_batch_t b, const double* theta, double* energies, double* grads) {
+  NvtxRange range("spz_batch_run");
   if (!b || !theta || !energies || (b->nparams_total && !grads)) return fail(SPZ_ERR_NULL, "NULL argument");
   std::memcpy(b->h_theta, theta, b->nparams_total * sizeof(double));
   if (!b->graph) {

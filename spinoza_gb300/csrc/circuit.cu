@@ -19,6 +19,7 @@
 
 #include <algorithm>
 #include <complex>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <vector>
@@ -1484,6 +1485,10 @@ int run_gates_io(spz_state_t h, const std::vector<GateApp>& gates_in, uint32_t f
   // are non-local in pass p (the tiles are selected by their index bits).
   auto launch_tiles = [&](size_t p, int part, int parts, int slab_q = -1) -> int {
     const PlannedPass& P = passes[p];
+    char label[96];
+    std::snprintf(label, sizeof label, "tile pass %zu: %zu ops, %zu local qubits, part %d of %d", p, counts[p],
+                  P.local.size(), part, parts);
+    NvtxRange range(label);
     PassArgs A{};
     A.re = h->re;
     A.im = h->im;
@@ -2162,6 +2167,7 @@ int spz_circuit_execute(spz_state_t h, const spz_op* ops, size_t nops, spz_track
   if (nops && !ops) return fail(SPZ_ERR_NULL, "ops is NULL");
   if (stats) std::memset(stats, 0, sizeof(*stats));
   if (int rc = settle(h)) return rc;  // measurements read the state
+  NvtxRange range("spz_circuit_execute");
   return execute(h, ops, nops, tracker, flags, stats);
 }
 
@@ -2172,6 +2178,7 @@ int spz_circuit_execute_host(spz_state_t h, const double* in_reals, const double
   if (nops && !ops) return fail(SPZ_ERR_NULL, "ops is NULL");
   if (stats) std::memset(stats, 0, sizeof(*stats));
   clear_factor(h);  // the handle's contents are replaced by the input arrays
+  NvtxRange range("spz_circuit_execute_host");
   auto pinned = [](const void* p) {
     cudaPointerAttributes a{};
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {

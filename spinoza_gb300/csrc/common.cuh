@@ -13,7 +13,33 @@
 
 #include "../../include/spinoza_gb300.h"
 
+// NVTX ranges (header-only NVTX 3): executor calls and fused passes show as
+// named host ranges under a profiler; without one the calls return at once.
+#if defined(__has_include)
+#if __has_include(<nvtx3/nvToolsExt.h>)
+#include <nvtx3/nvToolsExt.h>
+#define SPZ_HAVE_NVTX 1
+#endif
+#endif
+
 namespace spz {
+
+struct NvtxRange {
+  explicit NvtxRange(const char* name) {
+#ifdef SPZ_HAVE_NVTX
+    nvtxRangePushA(name);
+#else
+    (void)name;
+#endif
+  }
+  ~NvtxRange() {
+#ifdef SPZ_HAVE_NVTX
+    nvtxRangePop();
+#endif
+  }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 constexpr int kMaxQubits = SPZ_MAX_QUBITS;
 constexpr int kNumSMs = 152;          // GB300: 2 dies x 76 SMs
