@@ -289,6 +289,16 @@ int spz_program_destroy(spz_program_t p);
  * measurement outcome as 0.  For inspecting how a circuit is fused. */
 int spz_plan_stats(uint32_t n, const spz_op* ops, size_t nops, uint32_t flags, spz_exec_stats* stats);
 
+/* The passes spz_circuit_execute would launch (host only), one entry per
+ * pass as counted in spz_exec_stats.passes: local_mask[k] = the local qubits
+ * of a fused tile pass (0 for a plain one-gate pass or a measurement's two
+ * passes), pass_ops[k] = the device ops it applies (after the fast-mode
+ * lowering and fusion; 1 for a plain gate, 0 for a measurement's passes).
+ * *count receives the number of passes; at most `capacity` are written.
+ * For inspecting the plan (tile sizes, copy-overlap geometry). */
+int spz_plan_passes(uint32_t n, const spz_op* ops, size_t nops, uint32_t flags, uint64_t* local_mask,
+                    uint32_t* pass_ops, size_t capacity, size_t* count);
+
 /* The order in which spz_circuit_execute would apply `ops` (host only):
  * order[k] is the index of the k-th applied op and pass[k] the pass (kernel
  * launch) that applies it; skipped ops do not appear.  *count receives the

@@ -148,6 +148,8 @@ SIGNATURES = [
     ("spz_program_stats", c_int, [c_void_p, POINTER(spz_exec_stats)]),
     ("spz_program_destroy", c_int, [c_void_p]),
     ("spz_plan_stats", c_int, [c_uint32, c_void_p, c_size_t, c_uint32, POINTER(spz_exec_stats)]),
+    ("spz_plan_passes", c_int, [c_uint32, c_void_p, c_size_t, c_uint32, c_void_p, c_void_p, c_size_t,
+                                POINTER(c_size_t)]),
     ("spz_plan_schedule", c_int, [c_uint32, c_void_p, c_size_t, c_uint32, c_void_p, c_void_p, c_size_t,
                                   POINTER(c_size_t)]),
     ("spz_iqft", c_int, [c_void_p, c_void_p, c_uint32]),

@@ -400,6 +400,22 @@ def plan_schedule(n: int, ops: np.ndarray, fused: bool = True) -> tuple[np.ndarr
     return order[: count.value], passes[: count.value]
 
 
+def plan_passes(n: int, ops: np.ndarray, fused: bool = True, fast: bool = False,
+                extra_flags: int = 0) -> tuple[np.ndarray, np.ndarray]:
+    """(local_mask, pass_ops): per pass the executor would launch, the fused
+    tile pass's local qubits as a bit mask (0 for a plain one-gate pass or a
+    measurement's passes) and the device ops it applies (host only, no GPU)."""
+    ops = np.ascontiguousarray(ops, dtype=nat.OP_DTYPE)
+    flags = _flags(fused, fast) | int(extra_flags)
+    count = nat.c_size_t()
+    nat.check(nat.lib().spz_plan_passes(int(n), nat.ptr(ops), len(ops), flags, None, None, 0, byref(count)))
+    masks = np.zeros(count.value, dtype=np.uint64)
+    pass_ops = np.zeros(count.value, dtype=np.uint32)
+    nat.check(nat.lib().spz_plan_passes(int(n), nat.ptr(ops), len(ops), flags, nat.ptr(masks), nat.ptr(pass_ops),
+                                        count.value, byref(count)))
+    return masks, pass_ops
+
+
 def plan_stats(n: int, ops: np.ndarray, fused: bool = True, fast: bool = False) -> dict:
     """How the executor would fuse `ops` on n qubits (host only, no GPU)."""
     st = nat.spz_exec_stats()

@@ -1868,7 +1868,16 @@ int execute(spz_state_t h, const spz_op* ops, size_t nops, spz_tracker* tracker,
 
 // Plan without executing (host only): fills the counters run_gates would.
 int plan_stats(uint32_t n, const spz_op* ops, size_t nops, uint32_t flags, spz_exec_stats* st,
-               std::vector<uint32_t>* order = nullptr, std::vector<uint32_t>* pass_of = nullptr) {
+               std::vector<uint32_t>* order = nullptr, std::vector<uint32_t>* pass_of = nullptr,
+               std::vector<uint64_t>* masks = nullptr, std::vector<uint32_t>* pass_ops = nullptr) {
+  // masks / pass_ops: per pass (as counted in st->passes), the tile pass's
+  // local qubits (0: not a tile pass) and its device ops
+  auto record = [&](uint64_t mask, uint32_t count) {
+    if (masks) {
+      masks->push_back(mask);
+      pass_ops->push_back(count);
+    }
+  };
   spz_state_s fake;
   fake.n = n;
   fake.N = 1ull << n;
@@ -1892,6 +1901,7 @@ int plan_stats(uint32_t n, const spz_op* ops, size_t nops, uint32_t flags, spz_e
         }
         st->passes++;
         st->bytes_moved += gate_algorithmic_bytes(n, g);
+        record(0, 1);
       }
     } else {
       const int k = std::min<int>((int)n, kTileMaxK);
@@ -1901,14 +1911,20 @@ int plan_stats(uint32_t n, const spz_op* ops, size_t nops, uint32_t flags, spz_e
       pad_tile_passes(planned, n, k);
       std::vector<double> no_flat;
       for (const PlannedPass& P : planned) {
-        if ((fast || (flags & SPZ_EXEC_SHUFFLE)) &&
-            (P.gates.size() > 1 || P.gates[0].kind >= FK_LAZY_H || P.gates[0].cond >= 0)) {
+        const bool tiled = P.gates.size() > 1 || P.gates[0].kind >= FK_LAZY_H || P.gates[0].cond >= 0;
+        size_t device_ops = P.gates.size();
+        if ((fast || (flags & SPZ_EXEC_SHUFFLE) || masks) && tiled) {
           std::vector<TileGate> tg;
           for (const GateApp& g : P.gates) tg.push_back(tile_gate(g, P.local, &tables, &no_offsets));
           if (fast) st->fp64_ops -= fuse_lazy_pairs(tg, P.gates, tables, &no_flat, n);
           if (flags & SPZ_EXEC_SHUFFLE) st->shuffle_gates += mark_shuffle_runs(tg.data(), tg.size(), (int)P.local.size());
           no_flat.clear();
+          device_ops = tg.size();
         }
+        uint64_t L = 0;
+        if (tiled)
+          for (int q : P.local) L |= 1ull << q;
+        record(L, (uint32_t)device_ops);
         if (order && !fast)
           for (const GateApp& g : P.gates) {
             order->push_back((uint32_t)g.src);
@@ -1940,6 +1956,8 @@ int plan_stats(uint32_t n, const spz_op* ops, size_t nops, uint32_t flags, spz_e
           pass_of->push_back((uint32_t)st->passes);
         }
         st->passes += 2;
+        record(0, 0);
+        record(0, 0);
       }
       continue;
     }
@@ -2234,6 +2252,24 @@ int spz_plan_stats(uint32_t n, const spz_op* ops, size_t nops, uint32_t flags, s
   if (n == 0 || n > kMaxQubits) return fail(SPZ_ERR_INVALID_ARGUMENT, "n out of range");
   std::memset(stats, 0, sizeof(*stats));
   return plan_stats(n, ops, nops, flags, stats);
+}
+
+int spz_plan_passes(uint32_t n, const spz_op* ops, size_t nops, uint32_t flags, uint64_t* local_mask,
+                    uint32_t* pass_ops, size_t capacity, size_t* count) {
+  if (!count || (capacity && (!local_mask || !pass_ops))) return fail(SPZ_ERR_NULL, "NULL argument");
+  if (nops && !ops) return fail(SPZ_ERR_NULL, "ops is NULL");
+  if (n == 0 || n > kMaxQubits) return fail(SPZ_ERR_INVALID_ARGUMENT, "n out of range");
+  spz_exec_stats st{};
+  std::vector<uint64_t> m;
+  std::vector<uint32_t> c;
+  int rc = plan_stats(n, ops, nops, flags, &st, nullptr, nullptr, &m, &c);
+  if (rc) return rc;
+  *count = m.size();
+  for (size_t i = 0; i < m.size() && i < capacity; ++i) {
+    local_mask[i] = m[i];
+    pass_ops[i] = c[i];
+  }
+  return SPZ_OK;
 }
 
 int spz_plan_schedule(uint32_t n, const spz_op* ops, size_t nops, uint32_t flags, uint32_t* order, uint32_t* pass,

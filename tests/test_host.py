@@ -144,6 +144,42 @@ def test_planner_marks_shuffle_runs(native):
     assert st.shuffle_gates == 0
 
 
+def test_plan_passes_full_tiles_and_fused_ops(native):
+    """spz_plan_passes: one entry per counted pass; every tile pass of the
+    30-qubit brickwork holds 2^10 amplitudes; a circuit on five qubits gets a
+    single tile pass padded to 10 local qubits; in fast mode the fused lazy
+    pairs leave fewer device ops than lowered ops."""
+    n = 30
+    ops = brickwork_ops(n, 20)
+    for fast in (False, True):
+        masks, pops = circuit.plan_passes(n, ops, fast=fast)
+        st = circuit.plan_stats(n, ops, fast=fast)
+        assert len(masks) == st["passes"] and (masks != 0).sum() == st["tile_passes"]
+        assert all(bin(int(m)).count("1") == 10 and int(m) & 7 == 7 for m in masks if m)
+    _, exact_ops = circuit.plan_passes(n, ops)
+    _, fast_ops = circuit.plan_passes(n, ops, fast=True)
+    assert exact_ops.sum() == len(ops)
+    assert fast_ops.sum() < len(ops)  # 600 lazy rotations, most of them in fused pairs
+    # the trailing fast passes keep three consecutive high qubits non-local (the
+    # host-array execute downloads in their slab geometry)
+    masks, _ = circuit.plan_passes(n, ops, fast=True)
+    tail = int(masks[-1]) | int(masks[-2])
+    assert any(((tail >> q) & 7) == 0 for q in range(15, 25))
+    narrow = np.zeros(8, dtype=nat.OP_DTYPE)
+    for i in range(8):
+        narrow[i] = ((nat.H if i % 2 else nat.RY, 0, 0, 0, (0.3 * i, 0, 0)), i % 5, nat.CONTROLS_NONE, 0, 0)
+    masks, pops = circuit.plan_passes(n, narrow)
+    assert len(masks) == 1 and bin(int(masks[0])).count("1") == 10 and int(masks[0]) & 31 == 31
+    assert pops[0] == 8
+    # measurements: two passes each, no tile
+    m = np.zeros(3, dtype=nat.OP_DTYPE)
+    m[0] = ((nat.H, 0, 0, 0, (0, 0, 0)), 0, 0, 0, 0)
+    m[1] = ((nat.M, 0, 0, 0, (0.5, 0, 0)), 1, 0, 0, 0)
+    m[2] = ((nat.H, 0, 0, 0, (0, 0, 0)), 0, 0, 0, 0)
+    masks, pops = circuit.plan_passes(4, m)
+    assert list(pops) == [1, 0, 0, 1] and not masks.any()
+
+
 def random_ops(n, ngates, seed):
     """Every gate kind with none / single / ones / mixed controls."""
     r = np.random.default_rng(seed)
